@@ -1,0 +1,203 @@
+/* mclicks.h — C-ABI of the GB300 EM trainer for click models.
+ *
+ * This is the boundary below the reference's host C++ API (ClickModel_Hst,
+ * em_parallel, the mclicks CLI).  Every entry point takes plain pointers and
+ * sizes, returns an int status (MC_OK = 0) and leaves a message for
+ * mc_last_error() on failure; the reference instead printed and aborted
+ * (utils/utils.cuh:27-42, parallel_em/communicator.cpp:119-133).
+ *
+ * Each declaration names the reference interface it replaces (file:line
+ * within the reference project).  Streams are passed as `void*` holding a
+ * cudaStream_t (NULL = the legacy default stream); no call is re-entrant on
+ * one handle.
+ */
+#ifndef MCLICKS_H
+#define MCLICKS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MC_MAX_SERP 10           /* utils/definitions.h:50 */
+
+/* Model ids of --model-type (main.cpp:178-183). */
+enum { MC_PBM = 0, MC_CCM = 1, MC_DBN = 2, MC_UBM = 3 };
+
+/* Statistics mode.  PARITY reproduces the reference's CPU path, where a
+ * per-session statistic slot the E-step never writes keeps the default
+ * Param (1,2) (click_models/param.cuh:23-24, common.cu:57) and is summed
+ * every iteration (UBM examination slots, ubm.cu:222 with common.cu:161-163;
+ * DBN satisfaction of unclicked ranks, dbn.cu:358-376).  CLEAN sums only the
+ * slots that were written. */
+enum { MC_MODE_PARITY = 0, MC_MODE_CLEAN = 1 };
+
+/* EM implementation: one fused persistent kernel per iteration, or the plain
+ * two-kernel E-step + scatter of the reference's GPU path
+ * (parallel_em/kernel.cu:42-89) with the same statistics semantics. */
+enum { MC_IMPL_FUSED = 0, MC_IMPL_PLAIN = 1 };
+
+/* Status codes. */
+enum {
+    MC_OK = 0,
+    MC_ERR_INVALID = 1,   /* bad argument */
+    MC_ERR_IO = 2,        /* file could not be read or written */
+    MC_ERR_CUDA = 3,      /* a CUDA call failed */
+    MC_ERR_NOMEM = 4,     /* host or device allocation failed */
+    MC_ERR_STATE = 5,     /* call out of order (e.g. EM before upload) */
+    MC_ERR_DEVICE = 6     /* a kernel reported an error through its status word */
+};
+
+/* Copies the last error message of the calling thread into buf (always
+ * NUL-terminated); returns the last status code. */
+int mc_last_error(char* buf, size_t len);
+
+/* Library version string. */
+const char* mc_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Synthetic click logs (test and benchmark inputs).
+ * ------------------------------------------------------------------------- */
+typedef struct mc_synth_config {
+    int64_t n_sessions;      /* sessions to generate */
+    int32_t n_queries;       /* query ids are Zipf(zipf_s) over [0, n_queries) */
+    int32_t pool;            /* candidate docs per query (10..256) */
+    double zipf_s;
+    int32_t click_model;     /* ground truth: 0 PBM, 1 CCM, 2 DBN */
+    int32_t reserved;
+    double atr_beta_b;       /* attractiveness / relevance ~ Beta(1, b) */
+    double sat_beta_b;       /* DBN satisfaction ~ Beta(1, b) */
+    double gamma;            /* DBN continuation */
+    double tau1, tau2, tau3; /* CCM continuation */
+    double pbm_exam_scale;   /* PBM examination gamma_r = scale / sqrt(r + 1) */
+    uint64_t seed;
+} mc_synth_config;
+
+/* Fills c with one of three presets: 0 = 40k sessions / 1k queries Zipf 1.1 /
+ * 20-doc pools / PBM clicks; 1 = 2M / 100k / Zipf 1.0 / 30 / DBN clicks;
+ * 2 = 20M / 1M / Zipf 1.0 / 50 / CCM clicks. */
+void mc_synth_config_default(mc_synth_config* c, int preset);
+
+/* Sessions [first, first + count) in arrival order: query[count],
+ * docs[count * 10] (session-major), click_mask[count] (bit r = rank r). */
+int mc_synth_generate(const mc_synth_config* cfg, int64_t first, int64_t count,
+                      int32_t* query, int32_t* docs, uint16_t* click_mask);
+
+/* Writes n_sessions + 1 sessions in the reference's text log format
+ * (README.md:39-52); the reader keeps n_sessions of them (dataset.cpp:240-242). */
+int mc_synth_write_log(const mc_synth_config* cfg, const char* path);
+
+/* ---------------------------------------------------------------------------
+ * Dataset ingest (host).  Replaces Dataset::parse_dataset
+ * (data/dataset.cpp:421-455) for one worker: parse (dataset.cpp:224-305),
+ * tail test split (dataset.cpp:385-397), unstable std::sort of the training
+ * sessions by query (dataset.cpp:17-43), query-document indices in order of
+ * first appearance (dataset.cpp:314-339), test filtering
+ * (dataset.cpp:349-374).  Bit-exact with the reference.
+ * ------------------------------------------------------------------------- */
+typedef struct mc_dataset mc_dataset;
+
+int mc_dataset_parse(const char* path, int32_t max_sessions, float test_share, mc_dataset** out);
+
+/* Same split/sort/index steps on sessions already in memory, in arrival
+ * order (as the parser would have produced them). */
+int mc_dataset_from_sessions(int64_t n, const int32_t* query, const int32_t* docs,
+                             const uint16_t* click_mask, float test_share, mc_dataset** out);
+
+int mc_dataset_info(const mc_dataset* d, int64_t* n_train, int64_t* n_test, int64_t* n_qd);
+
+/* Copies one set out (which = 0 train, 1 test).  docs and pidx are
+ * session-major [n * 10]; pidx is -1 for a test doc unseen in training.
+ * Any output pointer may be NULL. */
+int mc_dataset_copy(const mc_dataset* d, int which, int32_t* query, int32_t* docs,
+                    int32_t* pidx, uint16_t* click_mask);
+
+void mc_dataset_free(mc_dataset* d);
+
+/* ---------------------------------------------------------------------------
+ * Click model on the GPU.
+ * ------------------------------------------------------------------------- */
+typedef struct mc_model mc_model;
+
+/* Replaces create_cm_host / create_cm_dev (click_models/base.cu:19-88) and
+ * Kernel::initialize (parallel_em/kernel.cu:24-33). */
+int mc_model_create(int model_type, int mode, int device, mc_model** out);
+
+/* Replaces convert_to_device (data/search.cu:342-356),
+ * allocate_memory_on_device (parallel_em/parallel_em.cu:281-309) and
+ * init_parameters (click_models/common.cu:31-61): uploads the training
+ * sessions (sorted by query, as ingest leaves them; pidx session-major
+ * [n * 10] in [0, n_qd)), builds the tile work queue and sets every
+ * parameter to the prior value 1/2. */
+int mc_model_upload(mc_model* m, int64_t n_train, const int32_t* query, const int32_t* pidx,
+                    const uint16_t* click_mask, int64_t n_qd, void* stream);
+
+/* Uploads the evaluation set (pidx may hold -1 for unseen docs). */
+int mc_model_upload_test(mc_model* m, int64_t n_test, const int32_t* pidx,
+                         const uint16_t* click_mask, void* stream);
+
+/* Tile shape of the fused kernel: sessions per tile, query-document window
+ * per tile (shared-memory privatisation width) and threads per block.
+ * 0 keeps the current value.  Rebuilds the work queue. */
+int mc_model_configure(mc_model* m, int32_t sessions_per_tile, int32_t window_qd, int32_t block_size);
+int mc_model_get_config(const mc_model* m, int32_t* sessions_per_tile, int32_t* window_qd, int32_t* block_size);
+
+/* Times a few fused iterations for each tile shape of a small grid and keeps
+ * the fastest.  Parameters are restored afterwards. */
+int mc_model_autotune(mc_model* m, void* stream);
+
+/* Runs n_iterations EM iterations: replaces the loop of em_parallel
+ * (parallel_em/parallel_em.cu:462-609): Kernel::em_training, reset_parameters,
+ * Kernel::update and the public-parameter sync.  The fused loop is captured
+ * once as a CUDA graph and replayed.  Asynchronous on `stream`. */
+int mc_model_em(mc_model* m, int32_t n_iterations, int impl, void* stream);
+
+/* The two halves of one plain iteration, for callers that drive the
+ * reference's process_session / update_parameters split
+ * (click_models/base.cuh:41-42). */
+int mc_model_process_sessions(mc_model* m, void* stream);
+int mc_model_update_parameters(mc_model* m, void* stream);
+
+/* Parameter arrays, in the order of ClickModel_Hst::get_parameters(ALL)
+ * (pbm.cu:305-321, ccm.cu:531-533, dbn.cu:535-538, ubm.cu:299-315):
+ *   PBM: examination[10], attractiveness[n_qd]
+ *   UBM: examination[55], attractiveness[n_qd]
+ *   DBN: attractiveness[n_qd], satisfaction[n_qd], continuation[1]
+ *   CCM: attractiveness[n_qd], continuation[3]
+ * is_public follows get_parameter_information (pbm.cu:120-132 etc.). */
+int mc_model_param_count(const mc_model* m);
+int mc_model_param_info(const mc_model* m, int index, char* name, size_t name_len,
+                        int64_t* size, int* is_public);
+
+/* Replaces transfer_parameters(D2H) + get_parameters (common.cu:93-102):
+ * copies the current parameter values (FP32, = Param::value(), param.cu:116-128)
+ * of array `index` to host memory.  Synchronous. */
+int mc_model_get_param(mc_model* m, int index, float* values, void* stream);
+
+/* Replaces set_parameters + transfer_parameters(H2D). */
+int mc_model_set_param(mc_model* m, int index, const float* values, void* stream);
+
+/* Replaces LogLikelihood::evaluate / Perplexity::evaluate
+ * (click_models/evaluation.cpp:25-66) on the GPU for the training (which = 0)
+ * or uploaded test (which = 1) set.  Outputs FP64 sums:
+ *   *ll_sum = sum over sessions of (sum_r log p_r) / 10      (p_r conditional)
+ *   log2_sums[r] = sum over sessions of log2 q_r             (q_r full)
+ *   *n_sessions = sessions evaluated.
+ * LL = ll_sum / n; perplexity at rank r = 2^(-log2_sums[r] / n)
+ * (parallel_em/parallel_em.cu:697-723).  Synchronous. */
+int mc_model_evaluate(mc_model* m, int which, double* ll_sum, double* log2_sums, int64_t* n_sessions,
+                      void* stream);
+
+/* Device memory held by the model, in bytes. */
+int mc_model_memory(const mc_model* m, int64_t* bytes);
+
+/* Replaces destroy_parameters (pbm.cu:445-460 etc.). */
+void mc_model_destroy(mc_model* m);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MCLICKS_H */

@@ -1,0 +1,60 @@
+// Launch entry points of the kernels, used by the host orchestration in model.cu.
+#ifndef MCLICKS_KERNELS_H
+#define MCLICKS_KERNELS_H
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace mcd {
+
+// ---- fused EM (em_fused.cu) -------------------------------------------------
+size_t fused_smem_bytes(int model, int window_max);
+cudaError_t fused_set_smem_limits(int window_max);
+cudaError_t fused_occupancy(int model, int block, int window_max, int* blocks_per_sm);
+cudaError_t launch_em_fused(int model, const FitDev* fits, const TileDev* tiles, int n_tiles, const SplitDev* splits,
+                            WorkState* ws, int window_max, int grid, int block, cudaStream_t stream);
+
+// ---- plain EM (em_plain.cu) -------------------------------------------------
+// The reference's 8-byte device record (data/search.cuh:63-73).
+struct PlainRec {
+    signed char click;
+    int pidx;
+};
+
+struct PlainArgs {
+    int64_t n, n_qd;
+    const PlainRec* recs;  // [10][n]
+    float2* atr2;          // [n_qd] (num, den)
+    float2* sat2;          // [n_qd] (DBN)
+    float2* pub2;          // [n_pub]
+    float2* tmp_atr;       // [10][n]
+    float2* tmp_sat;       // [10][n] (DBN)
+    float2* tmp_pub;       // [n_pub][n]
+};
+
+cudaError_t launch_plain_estep(int model, const PlainArgs& A, cudaStream_t st);
+cudaError_t launch_plain_reset(const PlainArgs& A, int n_pub, cudaStream_t st);
+cudaError_t launch_plain_update(int model, const PlainArgs& A, cudaStream_t st);
+cudaError_t launch_values_to_pairs(const float* v, float2* pairs, int64_t n, cudaStream_t st);
+cudaError_t launch_pairs_to_values(const float2* pairs, float* v, int64_t n, cudaStream_t st);
+cudaError_t launch_fill2(float2* p, int64_t n, float a, float b, cudaStream_t st);
+
+// ---- evaluation (eval.cu) ---------------------------------------------------
+struct EvalArgs {
+    int model;
+    int64_t n, stride, n_qd;
+    const int32_t* pidx;    // [10][stride]
+    const uint16_t* click;  // [n]
+    const float* atr;
+    const float* sat;
+    const float* pub;       // current public values
+    double* out;            // [11]: log-likelihood sum, then log2 sums per rank
+};
+
+cudaError_t launch_eval(const EvalArgs& A, int n_sm, cudaStream_t st);
+
+}  // namespace mcd
+
+#endif  // MCLICKS_KERNELS_H

@@ -1,0 +1,752 @@
+// mc_model_*: one click-model fit on one GPU.  Host orchestration of the
+// fused, plain and evaluation kernels behind the C-ABI (include/mclicks.h).
+//
+// Device layout of a fit (all resident in HBM):
+//   pidx      int32 [10][stride]   rank-major planes of parameter indices
+//   click     uint16 [n]           click bit masks
+//   cnt       uint2 [n_qd]         {occurrences, clicked occurrences} per qd
+//   atr, sat  float [n_qd]         current parameter values
+//   pub_theta float [2][128]       public values, double-buffered by iteration
+//   pub_bins  double [2 n_pub]     FP64 public statistic bins
+//   tiles     TileDev [n_tiles]    work queue (whole queries or query chunks)
+//   split_*   FP64 bins and counters of queries split over several tiles
+#include <algorithm>
+#include <climits>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "mclicks.h"
+#include "host_internal.h"
+#include "common.cuh"
+#include "kernels.h"
+
+using namespace mcd;
+using mch::set_error;
+
+namespace {
+
+int cuda_fail(const char* what, cudaError_t e) {
+    cudaGetLastError();
+    return set_error(e == cudaErrorMemoryAllocation ? MC_ERR_NOMEM : MC_ERR_CUDA,
+                     std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                             \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_fail(#call, e_);  \
+    } while (0)
+
+template <typename T>
+int dalloc(T** p, size_t count, int64_t* bytes) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) return cuda_fail("cudaMalloc", e);
+    *bytes += (int64_t)(count * sizeof(T));
+    return MC_OK;
+}
+
+template <typename T>
+void dfree(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+__global__ void pub_to_pairs_kernel(const float* theta, const int* iter, float2* pub2, int n_pub) {
+    int k = threadIdx.x;
+    if (k < n_pub) pub2[k] = make_float2(theta[(*iter & 1) * MC_MAX_PUB + k], 1.f);
+}
+
+__global__ void pairs_to_pub_kernel(const float2* pub2, float* theta, const int* iter, int n_pub) {
+    int k = threadIdx.x;
+    if (k < n_pub) {
+        float v = pub2[k].x / pub2[k].y;
+        theta[(*iter & 1) * MC_MAX_PUB + k] = v < MC_TOP ? v : MC_TOP;
+    }
+}
+
+struct ParamDesc {
+    const char* name;
+    int kind;  // 0 = public, 1 = attractiveness, 2 = satisfaction
+};
+
+}  // namespace
+
+struct mc_model {
+    int model = 0, mode = 0, device = 0, n_pub = 0, n_sm = 0;
+    int64_t n = 0, stride = 0, n_qd = 0, bytes = 0;
+    bool uploaded = false, fused_ok = false;
+    std::string fused_reason;
+    // query segments of the training set: sessions and qd range
+    std::vector<int64_t> seg_begin, seg_lo, seg_hi;
+    int spt = 512, wqd = 2048, block = 256;
+    // fused state
+    int32_t* d_pidx = nullptr;
+    uint16_t* d_click = nullptr;
+    uint2* d_cnt = nullptr;
+    float *d_atr = nullptr, *d_sat = nullptr, *d_pub_theta = nullptr;
+    double *d_pub_bins = nullptr, *d_pub_const = nullptr, *d_split_bins = nullptr;
+    unsigned *d_split_count = nullptr, *d_tiles_done = nullptr;
+    int *d_iter = nullptr, *d_status = nullptr;
+    FitDev* d_fit = nullptr;
+    TileDev* d_tiles = nullptr;
+    SplitDev* d_splits = nullptr;
+    WorkState* d_ws = nullptr;
+    int n_tiles = 0, n_splits = 0, grid = 0;
+    int64_t split_bins_count = 0;
+    int64_t tile_bytes = 0;
+    // plain state (allocated on first use)
+    PlainRec* d_recs = nullptr;
+    float2 *d_atr2 = nullptr, *d_sat2 = nullptr, *d_pub2 = nullptr, *d_tmp_atr = nullptr, *d_tmp_sat = nullptr,
+           *d_tmp_pub = nullptr;
+    int64_t plain_bytes = 0;
+    std::vector<PlainRec> h_recs_pending;
+    // evaluation set
+    int64_t n_test = 0, test_stride = 0;
+    int32_t* d_test_pidx = nullptr;
+    uint16_t* d_test_click = nullptr;
+    double* d_eval = nullptr;
+    int64_t test_bytes = 0;
+    // host copies kept for the plain path
+    std::vector<int32_t> h_pidx;
+    std::vector<uint16_t> h_click;
+    // graph of the fused loop
+    cudaGraphExec_t graph = nullptr;
+    int graph_iters = -1;
+    cudaStream_t own_stream = nullptr;
+
+    std::vector<ParamDesc> params() const {
+        switch (model) {
+            case MC_PBM: return {{"examination", 0}, {"attractiveness", 1}};
+            case MC_UBM: return {{"examination", 0}, {"attractiveness", 1}};
+            case MC_DBN: return {{"attractiveness", 1}, {"satisfaction", 2}, {"continuation", 0}};
+            default: return {{"attractiveness", 1}, {"continuation", 0}};
+        }
+    }
+
+    void drop_graph() {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        graph_iters = -1;
+    }
+
+    void free_tiles() {
+        dfree(d_tiles);
+        dfree(d_splits);
+        dfree(d_split_bins);
+        dfree(d_split_count);
+        bytes -= tile_bytes;
+        tile_bytes = 0;
+    }
+
+    void free_plain() {
+        dfree(d_recs); dfree(d_atr2); dfree(d_sat2); dfree(d_pub2); dfree(d_tmp_atr); dfree(d_tmp_sat); dfree(d_tmp_pub);
+        bytes -= plain_bytes;
+        plain_bytes = 0;
+    }
+
+    void free_train() {
+        drop_graph();
+        free_tiles();
+        free_plain();
+        dfree(d_pidx); dfree(d_click); dfree(d_cnt); dfree(d_atr); dfree(d_sat); dfree(d_pub_theta);
+        dfree(d_pub_bins); dfree(d_pub_const); dfree(d_tiles_done); dfree(d_iter); dfree(d_status);
+        dfree(d_fit); dfree(d_ws);
+        bytes = test_bytes;
+        uploaded = false;
+    }
+
+    void free_test() {
+        dfree(d_test_pidx); dfree(d_test_click); dfree(d_eval);
+        bytes -= test_bytes;
+        test_bytes = 0;
+        n_test = 0;
+    }
+
+    cudaStream_t pick(void* s) {
+        if (s) return (cudaStream_t)s;
+        if (!own_stream) cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking);
+        return own_stream;
+    }
+
+    int build_tiles();
+    int write_fit_desc();
+    int ensure_plain(cudaStream_t st);
+};
+
+// Splits the query segments into tiles of at most `spt` sessions and `wqd`
+// qd per window.  A query above either bound becomes a split query: chunks of
+// at most `spt` sessions that share FP64 bins.
+int mc_model::build_tiles() {
+    drop_graph();
+    free_tiles();
+    const int ns = private_stats(model);
+    std::vector<TileDev> tiles;
+    std::vector<SplitDev> splits;
+    int64_t bin_off = 0;
+    size_t n_seg = seg_lo.size();
+    TileDev cur{};
+    bool open = false;
+    auto close = [&]() {
+        if (open) tiles.push_back(cur);
+        open = false;
+    };
+    for (size_t g = 0; g < n_seg; g++) {
+        int64_t sb = seg_begin[g], sc = seg_begin[g + 1] - sb;
+        int64_t lo = seg_lo[g], hi = seg_hi[g];
+        if (sc > spt || hi - lo > wqd) {
+            close();
+            int nt = (int)((sc + spt - 1) / spt);
+            SplitDev sp;
+            sp.qd_begin = lo;
+            sp.qd_count = (int)(hi - lo);
+            sp.n_tiles = nt;
+            sp.bin_offset = bin_off;
+            bin_off += (hi - lo) * ns;
+            int sid = (int)splits.size();
+            splits.push_back(sp);
+            for (int k = 0; k < nt; k++) {
+                int64_t b = sb + sc * k / nt, e = sb + sc * (k + 1) / nt;
+                TileDev t{};
+                t.fit = 0;
+                t.split = sid;
+                t.s_begin = b;
+                t.s_count = (int)(e - b);
+                t.qd_begin = lo;
+                t.qd_count = (int)(hi - lo);
+                tiles.push_back(t);
+            }
+            continue;
+        }
+        if (open && (cur.s_count + sc > spt || hi - cur.qd_begin > wqd)) close();
+        if (!open) {
+            cur = TileDev{};
+            cur.fit = 0;
+            cur.split = -1;
+            cur.s_begin = sb;
+            cur.s_count = 0;
+            cur.qd_begin = lo;
+            open = true;
+        }
+        cur.s_count += (int)sc;
+        cur.qd_count = (int)(hi - cur.qd_begin);
+    }
+    close();
+    n_tiles = (int)tiles.size();
+    n_splits = (int)splits.size();
+    split_bins_count = bin_off;
+    int64_t before = bytes;
+    int rc;
+    if ((rc = dalloc(&d_tiles, tiles.size(), &bytes))) return rc;
+    if ((rc = dalloc(&d_splits, splits.size(), &bytes))) return rc;
+    if ((rc = dalloc(&d_split_bins, (size_t)bin_off, &bytes))) return rc;
+    if ((rc = dalloc(&d_split_count, splits.size(), &bytes))) return rc;
+    tile_bytes = bytes - before;
+    if (!tiles.empty()) CK(cudaMemcpy(d_tiles, tiles.data(), tiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice));
+    if (!splits.empty()) CK(cudaMemcpy(d_splits, splits.data(), splits.size() * sizeof(SplitDev), cudaMemcpyHostToDevice));
+    CK(cudaMemset(d_split_bins, 0, (size_t)std::max<int64_t>(bin_off, 1) * sizeof(double)));
+    CK(cudaMemset(d_split_count, 0, std::max<size_t>(splits.size(), 1) * sizeof(unsigned)));
+    CK(fused_set_smem_limits(wqd));
+    int per_sm = 0;
+    CK(fused_occupancy(model, block, wqd, &per_sm));
+    if (per_sm < 1) return set_error(MC_ERR_INVALID, "configuration does not fit on an SM (window or block too large)");
+    grid = std::max(1, std::min(n_tiles, per_sm * n_sm));
+    return write_fit_desc();
+}
+
+int mc_model::write_fit_desc() {
+    FitDev f{};
+    f.model = model;
+    f.mode = mode;
+    f.n = n;
+    f.stride = stride;
+    f.n_qd = n_qd;
+    f.n_tiles = n_tiles;
+    f.n_pub = n_pub;
+    f.pidx = d_pidx;
+    f.click = d_click;
+    f.cnt = d_cnt;
+    f.atr = d_atr;
+    f.sat = d_sat;
+    f.pub_theta = d_pub_theta;
+    f.pub_bins = d_pub_bins;
+    f.pub_const = d_pub_const;
+    f.split_bins = d_split_bins;
+    f.split_count = d_split_count;
+    f.tiles_done = d_tiles_done;
+    f.iter = d_iter;
+    f.status = d_status;
+    CK(cudaMemcpy(d_fit, &f, sizeof(f), cudaMemcpyHostToDevice));
+    return MC_OK;
+}
+
+int mc_model::ensure_plain(cudaStream_t st) {
+    if (d_recs) return MC_OK;
+    int64_t before = bytes;
+    int rc;
+    std::vector<PlainRec> recs((size_t)(n * MC_R));
+    for (int64_t s = 0; s < n; s++)
+        for (int r = 0; r < MC_R; r++) {
+            PlainRec& pr = recs[(size_t)(r * n + s)];
+            pr.click = (signed char)((h_click[(size_t)s] >> r) & 1u);
+            pr.pidx = h_pidx[(size_t)(s * MC_R + r)];
+        }
+    if ((rc = dalloc(&d_recs, recs.size(), &bytes))) return rc;
+    if ((rc = dalloc(&d_atr2, (size_t)n_qd, &bytes))) return rc;
+    if (model == MC_DBN && (rc = dalloc(&d_sat2, (size_t)n_qd, &bytes))) return rc;
+    if ((rc = dalloc(&d_pub2, (size_t)n_pub, &bytes))) return rc;
+    if ((rc = dalloc(&d_tmp_atr, (size_t)(n * MC_R), &bytes))) return rc;
+    if (model == MC_DBN && (rc = dalloc(&d_tmp_sat, (size_t)(n * MC_R), &bytes))) return rc;
+    if ((rc = dalloc(&d_tmp_pub, (size_t)(n * n_pub), &bytes))) return rc;
+    plain_bytes = bytes - before;
+    CK(cudaMemcpyAsync(d_recs, recs.data(), recs.size() * sizeof(PlainRec), cudaMemcpyHostToDevice, st));
+    // Temporaries the E-step never writes keep their initial value: the default
+    // Param (1, 2) in parity mode (common.cu:57), nothing in clean mode.
+    float a = mode == MC_MODE_PARITY ? 1.f : 0.f, b = mode == MC_MODE_PARITY ? 2.f : 0.f;
+    CK(launch_fill2(d_tmp_atr, n * MC_R, a, b, st));
+    if (d_tmp_sat) CK(launch_fill2(d_tmp_sat, n * MC_R, a, b, st));
+    CK(launch_fill2(d_tmp_pub, n * n_pub, a, b, st));
+    CK(cudaStreamSynchronize(st));
+    return MC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C-ABI
+// ---------------------------------------------------------------------------
+extern "C" int mc_model_create(int model_type, int mode, int device, mc_model** out) {
+    if (!out) return set_error(MC_ERR_INVALID, "model_create: null output");
+    *out = nullptr;
+    if (model_type < 0 || model_type > 3) return set_error(MC_ERR_INVALID, "model_create: model type must be 0..3");
+    if (mode != MC_MODE_PARITY && mode != MC_MODE_CLEAN) return set_error(MC_ERR_INVALID, "model_create: bad mode");
+    int count = 0;
+    CK(cudaGetDeviceCount(&count));
+    if (device < 0 || device >= count) return set_error(MC_ERR_INVALID, "model_create: no such device");
+    CK(cudaSetDevice(device));
+    mc_model* m = new (std::nothrow) mc_model();
+    if (!m) return set_error(MC_ERR_NOMEM, "model_create: out of host memory");
+    m->model = model_type;
+    m->mode = mode;
+    m->device = device;
+    m->n_pub = public_params(model_type);
+    cudaDeviceGetAttribute(&m->n_sm, cudaDevAttrMultiProcessorCount, device);
+    *out = m;
+    return MC_OK;
+}
+
+extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, const int32_t* pidx,
+                               const uint16_t* click, int64_t n_qd, void* stream) {
+    if (!m) return set_error(MC_ERR_INVALID, "model_upload: null model");
+    if (n < 0 || n_qd < 0 || n > (int64_t)1 << 31) return set_error(MC_ERR_INVALID, "model_upload: bad sizes");
+    if (n > 0 && (!query || !pidx || !click)) return set_error(MC_ERR_INVALID, "model_upload: null input");
+    for (int64_t i = 0; i < n * MC_R; i++)
+        if (pidx[i] < 0 || pidx[i] >= n_qd)
+            return set_error(MC_ERR_INVALID, "model_upload: parameter index out of [0, n_qd) at " + std::to_string(i));
+    CK(cudaSetDevice(m->device));
+    m->free_train();
+    cudaStream_t st = m->pick(stream);
+    m->n = n;
+    m->n_qd = n_qd;
+    m->stride = std::max<int64_t>(32, (n + 31) / 32 * 32);
+
+    // Query segments and their qd ranges.
+    m->seg_begin.clear(); m->seg_lo.clear(); m->seg_hi.clear();
+    m->fused_ok = true;
+    for (int64_t s = 0; s < n; s++) {
+        if (s == 0 || query[s] != query[s - 1]) {
+            m->seg_begin.push_back(s);
+            m->seg_lo.push_back(INT64_MAX);
+            m->seg_hi.push_back(INT64_MIN);
+        }
+        for (int r = 0; r < MC_R; r++) {
+            int64_t p = pidx[s * MC_R + r];
+            m->seg_lo.back() = std::min(m->seg_lo.back(), p);
+            m->seg_hi.back() = std::max(m->seg_hi.back(), p + 1);
+        }
+    }
+    m->seg_begin.push_back(n);
+    for (size_t g = 1; g < m->seg_lo.size(); g++)
+        if (m->seg_lo[g] < m->seg_hi[g - 1]) {
+            m->fused_ok = false;
+            m->fused_reason = "sessions are not grouped by query with per-query contiguous parameter indices "
+                              "(as Dataset::parse_dataset leaves them)";
+            break;
+        }
+
+    // Constant parts of the statistics.
+    std::vector<uint2> cnt((size_t)std::max<int64_t>(n_qd, 1), make_uint2(0, 0));
+    std::vector<double> pconst((size_t)(2 * m->n_pub), 0.0);
+    std::vector<int64_t> w(MC_UBM_SLOTS, 0), wc(MC_UBM_SLOTS, 0), clicked_r(MC_R, 0);
+    for (int64_t s = 0; s < n; s++) {
+        unsigned mk = click[s];
+        int last = 9, slot[MC_R];
+        for (int r = 0; r < MC_R; r++) {
+            uint2& c = cnt[(size_t)pidx[s * MC_R + r]];
+            c.x++;
+            if ((mk >> r) & 1u) { c.y++; clicked_r[r]++; }
+            slot[r] = r * (r + 1) / 2 + last;
+            if ((mk >> r) & 1u) last = r;
+        }
+        if (m->model == MC_UBM)
+            for (int r = 0; r < MC_R; r++) {
+                bool alive = true;
+                for (int r2 = r + 1; r2 < MC_R; r2++) alive = alive && slot[r2] != slot[r];
+                if (alive) { w[slot[r]]++; if ((mk >> r) & 1u) wc[slot[r]]++; }
+            }
+    }
+    for (int k = 0; k < m->n_pub; k++) {
+        double num = 1.0, den = 2.0;
+        if (m->model == MC_PBM) { num += (double)clicked_r[k]; den += (double)n; }
+        if (m->model == MC_UBM) {
+            num += (double)wc[k];
+            den += (double)w[k];
+            if (m->mode == MC_MODE_PARITY) { num += (double)(n - w[k]); den += 2.0 * (double)(n - w[k]); }
+        }
+        pconst[(size_t)(2 * k)] = num;
+        pconst[(size_t)(2 * k + 1)] = den;
+    }
+
+    // Rank-major planes.
+    std::vector<int32_t> planes((size_t)(m->stride * MC_R), 0);
+    for (int64_t s = 0; s < n; s++)
+        for (int r = 0; r < MC_R; r++) planes[(size_t)(r * m->stride + s)] = pidx[s * MC_R + r];
+    m->h_pidx.assign(pidx, pidx + n * MC_R);
+    m->h_click.assign(click, click + n);
+
+    int rc;
+    int64_t& B = m->bytes;
+    if ((rc = dalloc(&m->d_pidx, planes.size(), &B))) return rc;
+    if ((rc = dalloc(&m->d_click, (size_t)std::max<int64_t>(n, 1), &B))) return rc;
+    if ((rc = dalloc(&m->d_cnt, cnt.size(), &B))) return rc;
+    if ((rc = dalloc(&m->d_atr, (size_t)std::max<int64_t>(n_qd, 1), &B))) return rc;
+    if (m->model == MC_DBN && (rc = dalloc(&m->d_sat, (size_t)std::max<int64_t>(n_qd, 1), &B))) return rc;
+    if ((rc = dalloc(&m->d_pub_theta, 2 * MC_MAX_PUB, &B))) return rc;
+    if ((rc = dalloc(&m->d_pub_bins, (size_t)(2 * m->n_pub), &B))) return rc;
+    if ((rc = dalloc(&m->d_pub_const, (size_t)(2 * m->n_pub), &B))) return rc;
+    if ((rc = dalloc(&m->d_tiles_done, 1, &B))) return rc;
+    if ((rc = dalloc(&m->d_iter, 1, &B))) return rc;
+    if ((rc = dalloc(&m->d_status, 1, &B))) return rc;
+    if ((rc = dalloc(&m->d_fit, 1, &B))) return rc;
+    if ((rc = dalloc(&m->d_ws, 1, &B))) return rc;
+    CK(cudaMemcpyAsync(m->d_pidx, planes.data(), planes.size() * 4, cudaMemcpyHostToDevice, st));
+    if (n) CK(cudaMemcpyAsync(m->d_click, click, (size_t)n * 2, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(m->d_cnt, cnt.data(), cnt.size() * sizeof(uint2), cudaMemcpyHostToDevice, st));
+    std::vector<float> half((size_t)std::max<int64_t>(n_qd, 2 * MC_MAX_PUB), 0.5f);
+    CK(cudaMemcpyAsync(m->d_atr, half.data(), (size_t)std::max<int64_t>(n_qd, 1) * 4, cudaMemcpyHostToDevice, st));
+    if (m->d_sat) CK(cudaMemcpyAsync(m->d_sat, half.data(), (size_t)std::max<int64_t>(n_qd, 1) * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(m->d_pub_theta, half.data(), 2 * MC_MAX_PUB * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(m->d_pub_bins, 0, (size_t)(2 * m->n_pub) * 8, st));
+    CK(cudaMemcpyAsync(m->d_pub_const, pconst.data(), pconst.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(m->d_tiles_done, 0, 4, st));
+    CK(cudaMemsetAsync(m->d_iter, 0, 4, st));
+    CK(cudaMemsetAsync(m->d_status, 0, 4, st));
+    CK(cudaMemsetAsync(m->d_ws, 0, sizeof(WorkState), st));
+    CK(cudaStreamSynchronize(st));
+    m->uploaded = true;
+    if (m->fused_ok && (rc = m->build_tiles())) return rc;
+    return MC_OK;
+}
+
+extern "C" int mc_model_upload_test(mc_model* m, int64_t n, const int32_t* pidx, const uint16_t* click, void* stream) {
+    if (!m) return set_error(MC_ERR_INVALID, "model_upload_test: null model");
+    if (n < 0) return set_error(MC_ERR_INVALID, "model_upload_test: negative size");
+    if (n > 0 && (!pidx || !click)) return set_error(MC_ERR_INVALID, "model_upload_test: null input");
+    CK(cudaSetDevice(m->device));
+    m->free_test();
+    cudaStream_t st = m->pick(stream);
+    m->n_test = n;
+    m->test_stride = std::max<int64_t>(32, (n + 31) / 32 * 32);
+    std::vector<int32_t> planes((size_t)(m->test_stride * MC_R), -1);
+    for (int64_t s = 0; s < n; s++)
+        for (int r = 0; r < MC_R; r++) planes[(size_t)(r * m->test_stride + s)] = pidx[s * MC_R + r];
+    int64_t before = m->bytes;
+    int rc;
+    if ((rc = dalloc(&m->d_test_pidx, planes.size(), &m->bytes))) return rc;
+    if ((rc = dalloc(&m->d_test_click, (size_t)std::max<int64_t>(n, 1), &m->bytes))) return rc;
+    if ((rc = dalloc(&m->d_eval, MC_R + 1, &m->bytes))) return rc;
+    m->test_bytes = m->bytes - before;
+    CK(cudaMemcpyAsync(m->d_test_pidx, planes.data(), planes.size() * 4, cudaMemcpyHostToDevice, st));
+    if (n) CK(cudaMemcpyAsync(m->d_test_click, click, (size_t)n * 2, cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    return MC_OK;
+}
+
+extern "C" int mc_model_configure(mc_model* m, int32_t spt, int32_t wqd, int32_t block) {
+    if (!m) return set_error(MC_ERR_INVALID, "model_configure: null model");
+    if (spt < 0 || wqd < 0 || block < 0) return set_error(MC_ERR_INVALID, "model_configure: negative value");
+    if (block && (block % 32 || block > 512)) return set_error(MC_ERR_INVALID, "model_configure: block must be a multiple of 32, <= 512");
+    if (wqd && wqd > 24576) return set_error(MC_ERR_INVALID, "model_configure: window above 24576 qd");
+    if (spt && spt > (1 << 20)) return set_error(MC_ERR_INVALID, "model_configure: sessions per tile above 2^20");
+    CK(cudaSetDevice(m->device));
+    if (spt) m->spt = spt;
+    if (wqd) m->wqd = wqd;
+    if (block) m->block = block;
+    if (m->uploaded && m->fused_ok) return m->build_tiles();
+    return MC_OK;
+}
+
+extern "C" int mc_model_get_config(const mc_model* m, int32_t* spt, int32_t* wqd, int32_t* block) {
+    if (!m) return set_error(MC_ERR_INVALID, "model_get_config: null model");
+    if (spt) *spt = m->spt;
+    if (wqd) *wqd = m->wqd;
+    if (block) *block = m->block;
+    return MC_OK;
+}
+
+static int launch_fused_loop(mc_model* m, int iters, cudaStream_t st) {
+    for (int i = 0; i < iters; i++)
+        CK(launch_em_fused(m->model, m->d_fit, m->d_tiles, m->n_tiles, m->d_splits, m->d_ws, m->wqd, m->grid, m->block, st));
+    return MC_OK;
+}
+
+extern "C" int mc_model_em(mc_model* m, int32_t iters, int impl, void* stream) {
+    if (!m) return set_error(MC_ERR_INVALID, "model_em: null model");
+    if (!m->uploaded) return set_error(MC_ERR_STATE, "model_em: no training sessions uploaded");
+    if (iters < 0) return set_error(MC_ERR_INVALID, "model_em: negative iteration count");
+    if (impl != MC_IMPL_FUSED && impl != MC_IMPL_PLAIN) return set_error(MC_ERR_INVALID, "model_em: bad impl");
+    CK(cudaSetDevice(m->device));
+    cudaStream_t st = m->pick(stream);
+    if (iters == 0 || m->n == 0) return MC_OK;
+    if (impl == MC_IMPL_FUSED) {
+        if (!m->fused_ok) return set_error(MC_ERR_INVALID, "model_em: fused path unavailable: " + m->fused_reason);
+        if (!m->graph || m->graph_iters != iters) {
+            m->drop_graph();
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            int rc = launch_fused_loop(m, iters, st);
+            cudaError_t e = cudaStreamEndCapture(st, &g);
+            if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+            if (e != cudaSuccess) return cuda_fail("cudaStreamEndCapture", e);
+            e = cudaGraphInstantiate(&m->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { m->graph = nullptr; return cuda_fail("cudaGraphInstantiate", e); }
+            m->graph_iters = iters;
+        }
+        CK(cudaGraphLaunch(m->graph, st));
+    } else {
+        int rc = m->ensure_plain(st);
+        if (rc) return rc;
+        PlainArgs A{m->n, m->n_qd, m->d_recs, m->d_atr2, m->d_sat2, m->d_pub2, m->d_tmp_atr, m->d_tmp_sat, m->d_tmp_pub};
+        CK(launch_values_to_pairs(m->d_atr, m->d_atr2, m->n_qd, st));
+        if (m->d_sat) CK(launch_values_to_pairs(m->d_sat, m->d_sat2, m->n_qd, st));
+        pub_to_pairs_kernel<<<1, 64, 0, st>>>(m->d_pub_theta, m->d_iter, m->d_pub2, m->n_pub);
+        CK(cudaGetLastError());
+        for (int i = 0; i < iters; i++) {
+            CK(launch_plain_estep(m->model, A, st));
+            CK(launch_plain_reset(A, m->n_pub, st));
+            CK(launch_plain_update(m->model, A, st));
+        }
+        CK(launch_pairs_to_values(m->d_atr2, m->d_atr, m->n_qd, st));
+        if (m->d_sat) CK(launch_pairs_to_values(m->d_sat2, m->d_sat, m->n_qd, st));
+        pairs_to_pub_kernel<<<1, 64, 0, st>>>(m->d_pub2, m->d_pub_theta, m->d_iter, m->n_pub);
+        CK(cudaGetLastError());
+    }
+    if (!stream) CK(cudaStreamSynchronize(st));
+    return MC_OK;
+}
+
+extern "C" int mc_model_process_sessions(mc_model* m, void* stream) {
+    if (!m) return set_error(MC_ERR_INVALID, "process_sessions: null model");
+    if (!m->uploaded) return set_error(MC_ERR_STATE, "process_sessions: no training sessions uploaded");
+    CK(cudaSetDevice(m->device));
+    cudaStream_t st = m->pick(stream);
+    int rc = m->ensure_plain(st);
+    if (rc) return rc;
+    PlainArgs A{m->n, m->n_qd, m->d_recs, m->d_atr2, m->d_sat2, m->d_pub2, m->d_tmp_atr, m->d_tmp_sat, m->d_tmp_pub};
+    CK(launch_values_to_pairs(m->d_atr, m->d_atr2, m->n_qd, st));
+    if (m->d_sat) CK(launch_values_to_pairs(m->d_sat, m->d_sat2, m->n_qd, st));
+    pub_to_pairs_kernel<<<1, 64, 0, st>>>(m->d_pub_theta, m->d_iter, m->d_pub2, m->n_pub);
+    CK(cudaGetLastError());
+    CK(launch_plain_estep(m->model, A, st));
+    if (!stream) CK(cudaStreamSynchronize(st));
+    return MC_OK;
+}
+
+extern "C" int mc_model_update_parameters(mc_model* m, void* stream) {
+    if (!m) return set_error(MC_ERR_INVALID, "update_parameters: null model");
+    if (!m->uploaded || !m->d_recs) return set_error(MC_ERR_STATE, "update_parameters: call process_sessions first");
+    CK(cudaSetDevice(m->device));
+    cudaStream_t st = m->pick(stream);
+    PlainArgs A{m->n, m->n_qd, m->d_recs, m->d_atr2, m->d_sat2, m->d_pub2, m->d_tmp_atr, m->d_tmp_sat, m->d_tmp_pub};
+    CK(launch_plain_reset(A, m->n_pub, st));
+    CK(launch_plain_update(m->model, A, st));
+    CK(launch_pairs_to_values(m->d_atr2, m->d_atr, m->n_qd, st));
+    if (m->d_sat) CK(launch_pairs_to_values(m->d_sat2, m->d_sat, m->n_qd, st));
+    pairs_to_pub_kernel<<<1, 64, 0, st>>>(m->d_pub2, m->d_pub_theta, m->d_iter, m->n_pub);
+    CK(cudaGetLastError());
+    if (!stream) CK(cudaStreamSynchronize(st));
+    return MC_OK;
+}
+
+extern "C" int mc_model_param_count(const mc_model* m) { return m ? (int)m->params().size() : 0; }
+
+extern "C" int mc_model_param_info(const mc_model* m, int index, char* name, size_t name_len, int64_t* size, int* is_public) {
+    if (!m) return set_error(MC_ERR_INVALID, "param_info: null model");
+    auto ps = m->params();
+    if (index < 0 || index >= (int)ps.size()) return set_error(MC_ERR_INVALID, "param_info: index out of range");
+    if (name && name_len) {
+        std::strncpy(name, ps[(size_t)index].name, name_len - 1);
+        name[name_len - 1] = 0;
+    }
+    if (size) *size = ps[(size_t)index].kind == 0 ? m->n_pub : m->n_qd;
+    if (is_public) *is_public = ps[(size_t)index].kind == 0;
+    return MC_OK;
+}
+
+static int check_status(mc_model* m, cudaStream_t st) {
+    CK(cudaStreamSynchronize(st));
+    int status = 0;
+    CK(cudaMemcpy(&status, m->d_status, 4, cudaMemcpyDeviceToHost));
+    if (status) return set_error(MC_ERR_DEVICE, "kernel reported a parameter index outside its query's window (status " + std::to_string(status) + ")");
+    return MC_OK;
+}
+
+static int current_iter(mc_model* m, int* it) {
+    CK(cudaMemcpy(it, m->d_iter, 4, cudaMemcpyDeviceToHost));
+    return MC_OK;
+}
+
+extern "C" int mc_model_get_param(mc_model* m, int index, float* values, void* stream) {
+    if (!m || !values) return set_error(MC_ERR_INVALID, "get_param: null argument");
+    if (!m->uploaded) return set_error(MC_ERR_STATE, "get_param: no training sessions uploaded");
+    auto ps = m->params();
+    if (index < 0 || index >= (int)ps.size()) return set_error(MC_ERR_INVALID, "get_param: index out of range");
+    CK(cudaSetDevice(m->device));
+    cudaStream_t st = m->pick(stream);
+    int rc = check_status(m, st);
+    if (rc) return rc;
+    int kind = ps[(size_t)index].kind;
+    if (kind == 0) {
+        int it = 0;
+        if ((rc = current_iter(m, &it))) return rc;
+        CK(cudaMemcpy(values, m->d_pub_theta + (it & 1) * MC_MAX_PUB, (size_t)m->n_pub * 4, cudaMemcpyDeviceToHost));
+    } else if (m->n_qd) {
+        CK(cudaMemcpy(values, kind == 1 ? m->d_atr : m->d_sat, (size_t)m->n_qd * 4, cudaMemcpyDeviceToHost));
+    }
+    return MC_OK;
+}
+
+extern "C" int mc_model_set_param(mc_model* m, int index, const float* values, void* stream) {
+    if (!m || !values) return set_error(MC_ERR_INVALID, "set_param: null argument");
+    if (!m->uploaded) return set_error(MC_ERR_STATE, "set_param: no training sessions uploaded");
+    auto ps = m->params();
+    if (index < 0 || index >= (int)ps.size()) return set_error(MC_ERR_INVALID, "set_param: index out of range");
+    CK(cudaSetDevice(m->device));
+    cudaStream_t st = m->pick(stream);
+    CK(cudaStreamSynchronize(st));
+    int kind = ps[(size_t)index].kind;
+    if (kind == 0) {
+        int it = 0, rc;
+        if ((rc = current_iter(m, &it))) return rc;
+        CK(cudaMemcpy(m->d_pub_theta + (it & 1) * MC_MAX_PUB, values, (size_t)m->n_pub * 4, cudaMemcpyHostToDevice));
+    } else if (m->n_qd) {
+        CK(cudaMemcpy(kind == 1 ? m->d_atr : m->d_sat, values, (size_t)m->n_qd * 4, cudaMemcpyHostToDevice));
+    }
+    return MC_OK;
+}
+
+extern "C" int mc_model_evaluate(mc_model* m, int which, double* ll_sum, double* log2_sums, int64_t* n_sessions, void* stream) {
+    if (!m) return set_error(MC_ERR_INVALID, "evaluate: null model");
+    if (!m->uploaded) return set_error(MC_ERR_STATE, "evaluate: no training sessions uploaded");
+    if (which != 0 && which != 1) return set_error(MC_ERR_INVALID, "evaluate: which must be 0 (train) or 1 (test)");
+    CK(cudaSetDevice(m->device));
+    cudaStream_t st = m->pick(stream);
+    int rc = check_status(m, st);
+    if (rc) return rc;
+    int it = 0;
+    if ((rc = current_iter(m, &it))) return rc;
+    double out[MC_R + 1] = {0};
+    int64_t nn = which == 0 ? m->n : m->n_test;
+    if (nn > 0) {
+        if (!m->d_eval) {
+            int64_t before = m->bytes;
+            if ((rc = dalloc(&m->d_eval, MC_R + 1, &m->bytes))) return rc;
+            m->test_bytes += m->bytes - before;
+        }
+        EvalArgs A;
+        A.model = m->model;
+        A.n = nn;
+        A.stride = which == 0 ? m->stride : m->test_stride;
+        A.n_qd = m->n_qd;
+        A.pidx = which == 0 ? m->d_pidx : m->d_test_pidx;
+        A.click = which == 0 ? m->d_click : m->d_test_click;
+        A.atr = m->d_atr;
+        A.sat = m->d_sat;
+        A.pub = m->d_pub_theta + (it & 1) * MC_MAX_PUB;
+        A.out = m->d_eval;
+        CK(cudaMemsetAsync(m->d_eval, 0, (MC_R + 1) * 8, st));
+        CK(launch_eval(A, m->n_sm, st));
+        CK(cudaMemcpyAsync(out, m->d_eval, (MC_R + 1) * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    if (ll_sum) *ll_sum = out[0];
+    if (log2_sums) for (int r = 0; r < MC_R; r++) log2_sums[r] = out[1 + r];
+    if (n_sessions) *n_sessions = nn;
+    return MC_OK;
+}
+
+extern "C" int mc_model_autotune(mc_model* m, void* stream) {
+    if (!m) return set_error(MC_ERR_INVALID, "autotune: null model");
+    if (!m->uploaded || !m->fused_ok) return set_error(MC_ERR_STATE, "autotune: needs uploaded sessions and the fused path");
+    CK(cudaSetDevice(m->device));
+    cudaStream_t st = m->pick(stream);
+    CK(cudaStreamSynchronize(st));
+    // Snapshot of the state the trial iterations change.
+    std::vector<float> atr((size_t)std::max<int64_t>(m->n_qd, 1)), sat, th(2 * MC_MAX_PUB);
+    int it0 = 0;
+    CK(cudaMemcpy(atr.data(), m->d_atr, atr.size() * 4, cudaMemcpyDeviceToHost));
+    if (m->d_sat) { sat.resize(atr.size()); CK(cudaMemcpy(sat.data(), m->d_sat, sat.size() * 4, cudaMemcpyDeviceToHost)); }
+    CK(cudaMemcpy(th.data(), m->d_pub_theta, th.size() * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&it0, m->d_iter, 4, cudaMemcpyDeviceToHost));
+    struct Cand { int spt, wqd, block; };
+    const Cand cands[] = {{256, 2048, 128}, {512, 2048, 256}, {512, 4096, 256}, {1024, 4096, 256},
+                          {1024, 8192, 512}, {2048, 8192, 512}, {256, 1024, 256}};
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    Cand pick = {m->spt, m->wqd, m->block};
+    for (const Cand& c : cands) {
+        if (c.wqd * private_stats(m->model) * 4 > 200 * 1024) continue;
+        m->spt = c.spt; m->wqd = c.wqd; m->block = c.block;
+        if (m->build_tiles() != MC_OK) continue;
+        if (launch_fused_loop(m, 1, st) != MC_OK) continue;  // warm-up
+        CK(cudaEventRecord(e0, st));
+        if (launch_fused_loop(m, 3, st) != MC_OK) continue;
+        CK(cudaEventRecord(e1, st));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) { best = ms; pick = c; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    m->spt = pick.spt; m->wqd = pick.wqd; m->block = pick.block;
+    int rc = m->build_tiles();
+    if (rc) return rc;
+    CK(cudaMemcpy(m->d_atr, atr.data(), atr.size() * 4, cudaMemcpyHostToDevice));
+    if (m->d_sat) CK(cudaMemcpy(m->d_sat, sat.data(), sat.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(m->d_pub_theta, th.data(), th.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(m->d_iter, &it0, 4, cudaMemcpyHostToDevice));
+    return check_status(m, st);
+}
+
+extern "C" int mc_model_memory(const mc_model* m, int64_t* bytes) {
+    if (!m || !bytes) return set_error(MC_ERR_INVALID, "model_memory: null argument");
+    *bytes = m->bytes;
+    return MC_OK;
+}
+
+extern "C" void mc_model_destroy(mc_model* m) {
+    if (!m) return;
+    cudaSetDevice(m->device);
+    m->free_test();
+    m->free_train();
+    if (m->own_stream) cudaStreamDestroy(m->own_stream);
+    delete m;
+}

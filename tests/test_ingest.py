@@ -1,0 +1,117 @@
+"""Product ingest (mc_dataset_*) against the reference's partitions: parsing,
+the tail test split, the unstable sort by query, the qd indices and the test
+filtering must all be bit-exact."""
+import ctypes
+import tempfile
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import CASES, load_case
+from massiveclicks_gb300 import api, _capi
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_parse_matches_reference(name, native_lib):
+    case = load_case(name)
+    with tempfile.TemporaryDirectory() as tmp:
+        log = Path(tmp) / "log.txt"
+        log.write_bytes(case["log"].tobytes())
+        ds = api.Dataset.parse(str(log), int(case["max_sessions"]), float(case["test_share"]))
+    assert ds.n_qd == int(case["n_qd"])
+    for s, st in (("train", ds.train), ("test", ds.test)):
+        assert np.array_equal(st.query, case[f"{s}_query"]), (name, s, "query")
+        assert np.array_equal(st.docs, case[f"{s}_docs"]), (name, s, "docs")
+        assert np.array_equal(st.pidx, case[f"{s}_pidx"]), (name, s, "pidx")
+        assert np.array_equal(st.click, case[f"{s}_click"]), (name, s, "click")
+
+
+def _oracle_partition(cfg, tmp):
+    from oracle import bindings
+    log = Path(tmp) / "log.txt"
+    api.write_log(cfg, str(log))
+    return log, bindings.parse(str(log), cfg.n_sessions, 0.2)
+
+
+@pytest.mark.parametrize("preset,n,nq", [(0, 20000, 300), (1, 30000, 3000), (2, 30000, 5000)])
+def test_parse_matches_oracle_ingest(preset, n, nq, native_lib, oracle_lib):
+    """Larger logs than the fixtures, against the oracle's literal ingest
+    (std::sort over session records, map of maps)."""
+    cfg = api.synth_config(preset, n_sessions=n, n_queries=nq)
+    with tempfile.TemporaryDirectory() as tmp:
+        log, part = _oracle_partition(cfg, tmp)
+        ds = api.Dataset.parse(str(log), n, 0.2)
+    assert ds.n_qd == part["n_qd"]
+    for s, st in (("train", ds.train), ("test", ds.test)):
+        for k in ("query", "docs", "pidx", "click"):
+            assert np.array_equal(getattr(st, k), part[s][k]), (s, k)
+
+
+def test_from_sessions_equals_parse(native_lib):
+    cfg = api.synth_config(1, n_sessions=5000, n_queries=400)
+    q, d, m = api.synth_sessions(cfg)
+    with tempfile.TemporaryDirectory() as tmp:
+        log = Path(tmp) / "log.txt"
+        api.write_log(cfg, str(log))
+        a = api.Dataset.parse(str(log), cfg.n_sessions, 0.2)
+    b = api.Dataset.from_sessions(q, d, m, 0.2)
+    assert a.n_qd == b.n_qd
+    for s in ("train", "test"):
+        for k in ("query", "docs", "pidx", "click"):
+            assert np.array_equal(getattr(getattr(a, s), k), getattr(getattr(b, s), k))
+
+
+def test_split_counts(native_lib):
+    """n_train = int(n * (1 - t) - 0.5) + 1 (dataset.cpp:390), float product."""
+    cfg = api.synth_config(0, n_sessions=1000, n_queries=1)
+    q, d, m = api.synth_sessions(cfg)
+    for n, t in [(1000, 0.2), (999, 0.2), (7, 0.5), (1, 0.2), (10, 0.0), (10, 1.0)]:
+        ds = api.Dataset.from_sessions(q[:n], d[:n], m[:n], t)
+        expect = int(np.float32(n) * (np.float32(1.0) - np.float32(t)) - 0.5) + 1
+        assert len(ds.train) == min(expect, n)
+
+
+def test_sorted_and_contiguous(native_lib):
+    cfg = api.synth_config(2, n_sessions=20000, n_queries=2000)
+    q, d, m = api.synth_sessions(cfg)
+    ds = api.Dataset.from_sessions(q, d, m, 0.2)
+    assert np.all(np.diff(ds.train.query) >= 0)
+    # qd indices: first appearance order, so each query owns a contiguous range
+    lo = {}
+    hi = {}
+    for qq, p in zip(ds.train.query, ds.train.pidx):
+        lo[qq] = min(lo.get(qq, 1 << 30), p.min())
+        hi[qq] = max(hi.get(qq, -1), p.max())
+    keys = sorted(lo)
+    for a, b in zip(keys, keys[1:]):
+        assert hi[a] + 1 == lo[b]
+    assert ds.n_qd == hi[keys[-1]] + 1
+
+
+def test_missing_file_is_an_error(native_lib):
+    with pytest.raises(_capi.MCError) as e:
+        api.Dataset.parse("/nonexistent/path/log.txt", 10, 0.2)
+    assert e.value.code == 2
+
+
+def test_bad_test_share_is_an_error(native_lib):
+    with pytest.raises(_capi.MCError):
+        api.Dataset.from_sessions(np.zeros(1, np.int32), np.zeros((1, 10), np.int32), np.zeros(1, np.uint16), 1.5)
+
+
+def test_empty_log(native_lib):
+    with tempfile.TemporaryDirectory() as tmp:
+        log = Path(tmp) / "empty.txt"
+        log.write_text("")
+        ds = api.Dataset.parse(str(log), 100, 0.2)
+    assert len(ds.train) == 0 and len(ds.test) == 0 and ds.n_qd == 0
+
+
+def test_max_sessions_limits_reading(native_lib):
+    cfg = api.synth_config(0, n_sessions=500, n_queries=50)
+    with tempfile.TemporaryDirectory() as tmp:
+        log = Path(tmp) / "log.txt"
+        api.write_log(cfg, str(log))
+        ds = api.Dataset.parse(str(log), 100, 0.2)
+    assert len(ds.train) == 80
