@@ -1,0 +1,403 @@
+"""Benchmark: EM session-iterations/s of DBN on 20M synthetic sessions.
+
+Workload (one "step" = one EM iteration over all training sessions):
+  20,000,000 sessions over 1,000,000 queries (Zipf s = 1.0), 50-doc pools,
+  top-10 shown, clicks from a ground-truth CCM (tau = 0.6, 0.3, 0.2,
+  relevance ~ Beta(1, 3)); test share 0.2 -> 16,000,000 training sessions;
+  a DBN is fitted.  Inputs are seeded synthetic sessions of that shape (the
+  reference measured on the Yandex click log, which is not available here).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl ours` (default) prints one JSON line with the fused GPU throughput
+(`value`), the kernel's HBM roofline, the plain two-kernel GPU EM and the CPU
+baseline beside it, and an end-to-end number through the C-ABI with host
+buffers.  `--impl reference` times the reference's CPU training path (its
+restatement in oracle/, FP32, all host threads) on a bounded sample of the
+same workload.  Under torchrun (N > 1) every rank fits its own replica of the
+workload (weak scaling, no collective on the data path); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "EM session-iterations/s (20M sessions, DBN)"
+UNIT = "session-iterations/s"
+DATA = ("synthetic: 20M sessions, 1M queries Zipf(1.0), 50-doc pools, top-10 shown, ground-truth CCM clicks "
+        "(tau 0.6/0.3/0.2, relevance Beta(1,3)), seeded; test share 0.2")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--sessions", type=int, default=20_000_000)
+    ap.add_argument("--queries", type=int, default=1_000_000)
+    ap.add_argument("--cpu-sample", type=int, default=1_000_000,
+                    help="training sessions in the CPU baseline's bounded sample")
+    ap.add_argument("--e2e-iters", type=int, default=50)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing
+# ---------------------------------------------------------------------------
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    def __init__(self, world: int, backend: str):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        dev = "cuda" if self.pg.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def make_dataset(args, rank: int):
+    from massiveclicks_gb300 import api
+    cfg = api.synth_config(2, n_sessions=args.sessions, n_queries=args.queries)
+    cfg.seed = cfg.seed + 1000 * rank
+    t0 = time.perf_counter()
+    q, d, m = api.synth_sessions(cfg)
+    t1 = time.perf_counter()
+    ds = api.Dataset.from_sessions(q, d, m, 0.2)
+    t2 = time.perf_counter()
+    del q, d, m
+    return ds, {"generate_s": round(t1 - t0, 3), "ingest_s": round(t2 - t1, 3)}
+
+
+def cpu_sample(ds, n_sample: int):
+    """A query-aligned prefix of the sorted training set."""
+    n = min(n_sample, len(ds.train))
+    q = ds.train.query
+    while 0 < n < len(q) and q[n] == q[n - 1]:
+        n += 1
+    return n
+
+
+def time_cpu_oracle(ds, n: int, iters: int, warmup: int, threads: int):
+    """The reference's CPU path (FP32 restatement, reference threading) on the
+    first n training sessions: seconds per iteration, one entry per step."""
+    from oracle import bindings
+    sub = ds.train
+    nq = int(sub.pidx[:n].max()) + 1 if n else 0
+    fit = bindings.OracleFit("f32", 2, 0, sub.query[:n], sub.pidx[:n], sub.click[:n], nq)
+    fit.run(warmup, threads)
+    times = []
+    for _ in range(iters):
+        t0 = time.perf_counter()
+        fit.run(1, threads)
+        times.append(time.perf_counter() - t0)
+    return times
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for row in self.rows:
+            try:
+                sm.append(float(row[1]))
+                mx.append(float(row[2]))
+            except (ValueError, IndexError):
+                continue
+            for name, val in zip(names, row[5:9]):
+                if val.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {}
+
+
+def profile_traffic() -> dict | None:
+    """DRAM bytes per launch of the fused kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "em_fused_dbn_traffic.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return None
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    ds, prep = make_dataset(args, 0)
+    n = cpu_sample(ds, args.cpu_sample)
+    times = time_cpu_oracle(ds, n, args.steps, max(1, min(args.warmup, 2)), threads)
+    total = sum(times)
+    value = n * len(times) / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": DATA,
+        "config": {"workload": "DBN EM, 20M sessions (16M train), one EM iteration per step; "
+                               f"each step times a bounded sample of {n} training sessions",
+                   "sessions": args.sessions, "train_sessions": len(ds.train), "sample_sessions": n,
+                   "parallelism": f"{threads} host threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"first {n} training sessions (query-aligned) of the 16M, {len(times)} iterations"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank: int, world: int, local: int):
+    import torch
+    from massiveclicks_gb300 import api
+    from massiveclicks_gb300._capi import IMPL_FUSED, IMPL_PLAIN
+
+    torch.cuda.set_device(local)
+    dist = Dist(world, "nccl")
+    ds, prep = make_dataset(args, rank)
+    n_train, n_qd = len(ds.train), ds.n_qd
+    stream = torch.cuda.Stream()
+
+    cm = api.DBNModel(device=local)
+    t0 = time.perf_counter()
+    cm.upload(ds.train, n_qd, stream)
+    cm.upload_test(ds.test, stream)
+    prep["upload_s"] = round(time.perf_counter() - t0, 3)
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        cm.autotune(stream)
+        prep["autotune_s"] = round(time.perf_counter() - t0, 3)
+    spt, wqd, block = cm.get_config()
+
+    # ---- fused: warm-up, then exactly K timed iterations -------------------
+    cm.em(args.warmup, IMPL_FUSED, stream)
+    torch.cuda.synchronize()
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    cm.em(args.steps, IMPL_FUSED, stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    dist.barrier()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    ms_max = dist.max(ms)
+    value = world * n_train / (ms_max / 1000.0)
+
+    # ---- roofline of the fused kernel (one launch = one iteration) ----------
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    bytes_sessions = 42 * n_train          # int32 pidx x10 + uint16 click mask
+    bytes_params = 24 * n_qd               # read atr, sat, counts (16 B) + write atr, sat (8 B)
+    algo_bytes = bytes_sessions + bytes_params
+    achieved = algo_bytes / (ms / 1000.0) / 1e9
+    tr = profile_traffic()
+    traffic = None
+    if tr and tr.get("n_train") and tr.get("bytes_per_launch"):
+        traffic = tr["bytes_per_launch"] * n_train / tr["n_train"]
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm if hbm else 6800.0, "unit": "GB/s",
+                "frac": achieved / (hbm if hbm else 6800.0), "traffic": traffic,
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "fallback 6.8 TB/s",
+                "algorithmic_bytes_per_launch": algo_bytes,
+                "bytes_model": "42 B/session (pidx int32 x10 + uint16 clicks) + 24 B/qd (read atr, sat, counts; write atr, sat)"}
+
+    out = {}
+    if rank == 0:
+        # ---- equal test LL: fused vs plain from the prior, same iterations --
+        ll_iters = 10
+        cm.reset_to_prior(stream)
+        cm.em(ll_iters, IMPL_FUSED, stream)
+        torch.cuda.synchronize()
+        ev_f = cm.evaluate(1, stream)
+        if not args.no_plain:
+            cm.reset_to_prior(stream)
+            cm.em(1, IMPL_PLAIN, stream)   # allocates the plain buffers; warm-up
+            torch.cuda.synchronize()
+            p0 = torch.cuda.Event(enable_timing=True)
+            p1 = torch.cuda.Event(enable_timing=True)
+            plain_steps = 3
+            p0.record(stream)
+            cm.em(plain_steps, IMPL_PLAIN, stream)
+            p1.record(stream)
+            torch.cuda.synchronize()
+            plain_ms = p0.elapsed_time(p1) / plain_steps
+            cm.reset_to_prior(stream)
+            cm.em(ll_iters, IMPL_PLAIN, stream)
+            torch.cuda.synchronize()
+            ev_p = cm.evaluate(1, stream)
+            out["plain_gpu"] = {"value": n_train / (plain_ms / 1000.0), "unit": UNIT, "ms_per_step": plain_ms,
+                                "steps": plain_steps, "fused_speedup": plain_ms / ms}
+            out["test_llh"] = {"iterations": ll_iters, "fused": ev_f.llh, "plain": ev_p.llh,
+                               "rel_diff": abs(ev_f.llh - ev_p.llh) / abs(ev_p.llh),
+                               "fused_perplexity": ev_f.perplexity, "plain_perplexity": ev_p.perplexity}
+        else:
+            out["test_llh"] = {"iterations": ll_iters, "fused": ev_f.llh, "fused_perplexity": ev_f.perplexity}
+
+    # ---- end to end through the C-ABI with pinned host buffers --------------
+    e2e = None
+    if not args.no_e2e:
+        pq = torch.from_numpy(ds.train.query).pin_memory()
+        pp = torch.from_numpy(ds.train.pidx.reshape(-1)).pin_memory()
+        pm = torch.from_numpy(ds.train.click.view(np.int16)).pin_memory()
+        sizes = [(name, size) for name, size, _ in cm.parameter_information()]
+        host_out = {name: torch.empty(size, dtype=torch.float32).pin_memory() for name, size in sizes}
+        lib = api._capi.load()
+        h2d = pq.numel() * 4 + pp.numel() * 4 + pm.numel() * 2
+        d2h = sum(size * 4 for _, size in sizes)
+        import ctypes as C
+
+        def e2e_step():
+            m2 = C.c_void_p()
+            api.check(lib.mc_model_create(2, 0, local, C.byref(m2)))
+            api.check(lib.mc_model_upload(m2, n_train, C.c_void_p(pq.data_ptr()), C.c_void_p(pp.data_ptr()),
+                                          C.c_void_p(pm.data_ptr()), n_qd, C.c_void_p(stream.cuda_stream)))
+            api.check(lib.mc_model_configure(m2, spt, wqd, block))
+            api.check(lib.mc_model_em(m2, args.e2e_iters, IMPL_FUSED, C.c_void_p(stream.cuda_stream)))
+            for i, (name, _) in enumerate(sizes):
+                api.check(lib.mc_model_get_param(m2, i, C.c_void_p(host_out[name].data_ptr()),
+                                                 C.c_void_p(stream.cuda_stream)))
+            lib.mc_model_destroy(m2)
+
+        e2e_step()  # warm-up
+        torch.cuda.synchronize()
+        dist.barrier()
+        e2e_steps = 2
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_s = dist.max((time.perf_counter() - t0) / e2e_steps)
+        e2e = {"value": world * n_train * args.e2e_iters / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_s,
+               "step": f"mc_model_create + mc_model_upload (pinned host sessions) + {args.e2e_iters} fused "
+                       "iterations + mc_model_get_param of every array + destroy"}
+
+    cpu = None
+    if rank == 0:
+        threads = os.cpu_count() or 1
+        n = cpu_sample(ds, args.cpu_sample)
+        times = time_cpu_oracle(ds, n, 2, 1, threads)
+        cpu = {"value": n * len(times) / sum(times), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"first {n} training sessions (query-aligned), {len(times)} iterations after 1 warm-up; "
+                         "FP32 restatement of the reference's CPU path with its threading"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": DATA,
+            "config": {"workload": "DBN EM over 16M training sessions (20M sessions, test share 0.2); "
+                                   "one fused kernel launch per iteration, replayed from a CUDA graph",
+                       "sessions": args.sessions, "train_sessions": n_train, "n_qd": n_qd,
+                       "model": "DBN", "mode": "parity", "tile": {"sessions_per_tile": spt, "window_qd": wqd,
+                                                                   "block": block},
+                       "l2": "inputs larger than L2 (sessions 672 MB + parameters), no flush",
+                       "parallelism": "replicas" if world > 1 else "single GPU", "prep": prep},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": args.steps,
+            "clocks": clk,
+        }
+        line.update(out)
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

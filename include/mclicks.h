@@ -138,6 +138,11 @@ int mc_model_upload(mc_model* m, int64_t n_train, const int32_t* query, const in
 int mc_model_upload_test(mc_model* m, int64_t n_test, const int32_t* pidx,
                          const uint16_t* click_mask, void* stream);
 
+/* Replaces the value initialisation of init_parameters
+ * (click_models/common.cu:31-61): every parameter back to the prior 1/2 and
+ * the iteration counter to 0, keeping the uploaded sessions. */
+int mc_model_init_parameters(mc_model* m, void* stream);
+
 /* Tile shape of the fused kernel: sessions per tile, query-document window
  * per tile (shared-memory privatisation width) and threads per block.
  * 0 keeps the current value.  Rebuilds the work queue. */

@@ -44,6 +44,7 @@ _SIGS = {
     "mc_model_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(_VP)]),
     "mc_model_upload": (C.c_int, [_VP, _I64, _VP, _VP, _VP, _I64, _VP]),
     "mc_model_upload_test": (C.c_int, [_VP, _I64, _VP, _VP, _VP]),
+    "mc_model_init_parameters": (C.c_int, [_VP, _VP]),
     "mc_model_configure": (C.c_int, [_VP, _I32, _I32, _I32]),
     "mc_model_get_config": (C.c_int, [_VP, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32)]),
     "mc_model_autotune": (C.c_int, [_VP, _VP]),
@@ -81,10 +82,10 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     if _lib is not None:
         return _lib
     path = lib_path()
-    if not path.exists():
-        if not build_if_missing:
-            raise FileNotFoundError(f"{path} is not built")
-        _build.build_library()
+    if build_if_missing:
+        _build.build_library()  # no-op when the sources are unchanged
+    elif not path.exists():
+        raise FileNotFoundError(f"{path} is not built")
     lib = C.CDLL(str(path))
     for name, (res, args) in _SIGS.items():
         fn = getattr(lib, name)

@@ -187,6 +187,10 @@ class ClickModel:
         self.upload(dataset.train, dataset.n_qd, stream)
         self.upload_test(dataset.test, stream)
 
+    def reset_to_prior(self, stream=None) -> None:
+        """Every parameter back to 1/2, iteration counter to 0."""
+        check(_capi.load().mc_model_init_parameters(self._h, _stream(stream)))
+
     # -- tiling / tuning ----------------------------------------------------------
     def configure(self, sessions_per_tile: int = 0, window_qd: int = 0, block_size: int = 0) -> None:
         check(_capi.load().mc_model_configure(self._h, sessions_per_tile, window_qd, block_size))

@@ -309,6 +309,18 @@ cudaError_t launch_pairs_to_values(const float2* pairs, float* v, int64_t n, cud
     return cudaGetLastError();
 }
 
+__global__ void fill_value_kernel(float* p, int64_t n, float v) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) p[i] = v;
+}
+
+cudaError_t launch_fill_value(float* p, int64_t n, float v, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    fill_value_kernel<<<grid_for(n, 256, 8192), 256, 0, st>>>(p, n, v);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_fill2(float2* p, int64_t n, float a, float b, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     fill2_kernel<<<grid_for(n, 256, 8192), 256, 0, st>>>(p, n, a, b);

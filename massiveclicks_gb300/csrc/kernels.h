@@ -40,6 +40,7 @@ cudaError_t launch_plain_update(int model, const PlainArgs& A, cudaStream_t st);
 cudaError_t launch_values_to_pairs(const float* v, float2* pairs, int64_t n, cudaStream_t st);
 cudaError_t launch_pairs_to_values(const float2* pairs, float* v, int64_t n, cudaStream_t st);
 cudaError_t launch_fill2(float2* p, int64_t n, float a, float b, cudaStream_t st);
+cudaError_t launch_fill_value(float* p, int64_t n, float v, cudaStream_t st);
 
 // ---- evaluation (eval.cu) ---------------------------------------------------
 struct EvalArgs {

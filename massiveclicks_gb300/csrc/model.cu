@@ -71,6 +71,88 @@ __global__ void pairs_to_pub_kernel(const float2* pub2, float* theta, const int*
     }
 }
 
+// One pass over the uploaded sessions (session-major pidx): range check,
+// transposition into rank-major planes, per-qd occurrence / click counts, the
+// qd range of each query segment, and the click counts behind the public
+// constants (PBM: clicks per rank; UBM: written and clicked-written slots).
+__global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32_t* __restrict__ pidx_sm,
+                            const uint16_t* __restrict__ click, const int64_t* __restrict__ seg_begin, int64_t n_seg,
+                            int model, int32_t* planes, uint2* cnt, int* seg_lo, int* seg_hi,
+                            unsigned long long* pub_counts, int* flag) {
+    __shared__ unsigned int sc[2 * MC_UBM_SLOTS];
+    for (int k = threadIdx.x; k < 2 * MC_UBM_SLOTS; k += blockDim.x) sc[k] = 0;
+    __syncthreads();
+    const int64_t step = (int64_t)gridDim.x * blockDim.x;
+    const int64_t base = (int64_t)blockIdx.x * blockDim.x;
+    for (int64_t s0 = base; s0 < n; s0 += step) {
+        int64_t s = s0 + threadIdx.x;
+        bool valid = s < n;
+        int lo = INT_MAX, hi = INT_MIN;
+        int64_t seg = -1;
+        if (valid) {
+            unsigned m = click[s];
+            int64_t a = 0, b = n_seg - 1;  // last segment with begin <= s
+            while (a < b) {
+                int64_t mid = (a + b + 1) / 2;
+                if (seg_begin[mid] <= s) a = mid; else b = mid - 1;
+            }
+            seg = a;
+            int last = 9, slot[MC_R];
+#pragma unroll
+            for (int r = 0; r < MC_R; r++) {
+                int p = pidx_sm[s * MC_R + r];
+                if (p < 0 || (int64_t)p >= n_qd) { atomicOr(flag, 1); p = 0; }
+                planes[(int64_t)r * stride + s] = p;
+                bool c = (m >> r) & 1u;
+                atomicAdd(&cnt[p].x, 1u);
+                if (c) atomicAdd(&cnt[p].y, 1u);
+                lo = min(lo, p);
+                hi = max(hi, p + 1);
+                slot[r] = r * (r + 1) / 2 + last;
+                if (c) last = r;
+                if (model == 0 && c) atomicAdd(&sc[r], 1u);
+            }
+            if (model == 3) {
+#pragma unroll
+                for (int r = 0; r < MC_R; r++) {
+                    bool alive = true;
+#pragma unroll
+                    for (int r2 = r + 1; r2 < MC_R; r2++) alive = alive && slot[r2] != slot[r];
+                    if (alive) {
+                        atomicAdd(&sc[slot[r]], 1u);
+                        if ((m >> r) & 1u) atomicAdd(&sc[MC_UBM_SLOTS + slot[r]], 1u);
+                    }
+                }
+            }
+        }
+        // Segment ranges, aggregated over the lanes of a warp that share a segment.
+        unsigned peers = __match_any_sync(0xffffffffu, (unsigned long long)seg);
+        int wlo = __reduce_min_sync(peers, lo);
+        int whi = __reduce_max_sync(peers, hi);
+        if (valid && (threadIdx.x & 31) == __ffs(peers) - 1) {
+            atomicMin(&seg_lo[seg], wlo);
+            atomicMax(&seg_hi[seg], whi);
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 2 * MC_UBM_SLOTS; k += blockDim.x)
+        if (sc[k]) atomicAdd(&pub_counts[k], (unsigned long long)sc[k]);
+}
+
+// The plain path's 8-byte rank-major records, built from the planes.
+__global__ void build_recs_kernel(int64_t n, int64_t stride, const int32_t* planes, const uint16_t* click, PlainRec* recs) {
+    int64_t step = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += step) {
+        unsigned m = click[s];
+        for (int r = 0; r < MC_R; r++) {
+            PlainRec pr;
+            pr.click = (signed char)((m >> r) & 1u);
+            pr.pidx = planes[(int64_t)r * stride + s];
+            recs[(int64_t)r * n + s] = pr;
+        }
+    }
+}
+
 struct ParamDesc {
     const char* name;
     int kind;  // 0 = public, 1 = attractiveness, 2 = satisfaction
@@ -106,16 +188,12 @@ struct mc_model {
     float2 *d_atr2 = nullptr, *d_sat2 = nullptr, *d_pub2 = nullptr, *d_tmp_atr = nullptr, *d_tmp_sat = nullptr,
            *d_tmp_pub = nullptr;
     int64_t plain_bytes = 0;
-    std::vector<PlainRec> h_recs_pending;
     // evaluation set
     int64_t n_test = 0, test_stride = 0;
     int32_t* d_test_pidx = nullptr;
     uint16_t* d_test_click = nullptr;
     double* d_eval = nullptr;
     int64_t test_bytes = 0;
-    // host copies kept for the plain path
-    std::vector<int32_t> h_pidx;
-    std::vector<uint16_t> h_click;
     // graph of the fused loop
     cudaGraphExec_t graph = nullptr;
     int graph_iters = -1;
@@ -290,14 +368,7 @@ int mc_model::ensure_plain(cudaStream_t st) {
     if (d_recs) return MC_OK;
     int64_t before = bytes;
     int rc;
-    std::vector<PlainRec> recs((size_t)(n * MC_R));
-    for (int64_t s = 0; s < n; s++)
-        for (int r = 0; r < MC_R; r++) {
-            PlainRec& pr = recs[(size_t)(r * n + s)];
-            pr.click = (signed char)((h_click[(size_t)s] >> r) & 1u);
-            pr.pidx = h_pidx[(size_t)(s * MC_R + r)];
-        }
-    if ((rc = dalloc(&d_recs, recs.size(), &bytes))) return rc;
+    if ((rc = dalloc(&d_recs, (size_t)(n * MC_R), &bytes))) return rc;
     if ((rc = dalloc(&d_atr2, (size_t)n_qd, &bytes))) return rc;
     if (model == MC_DBN && (rc = dalloc(&d_sat2, (size_t)n_qd, &bytes))) return rc;
     if ((rc = dalloc(&d_pub2, (size_t)n_pub, &bytes))) return rc;
@@ -305,7 +376,10 @@ int mc_model::ensure_plain(cudaStream_t st) {
     if (model == MC_DBN && (rc = dalloc(&d_tmp_sat, (size_t)(n * MC_R), &bytes))) return rc;
     if ((rc = dalloc(&d_tmp_pub, (size_t)(n * n_pub), &bytes))) return rc;
     plain_bytes = bytes - before;
-    CK(cudaMemcpyAsync(d_recs, recs.data(), recs.size() * sizeof(PlainRec), cudaMemcpyHostToDevice, st));
+    if (n) {
+        build_recs_kernel<<<(int)std::min<int64_t>((n + 255) / 256, 8 * n_sm), 256, 0, st>>>(n, stride, d_pidx, d_click, d_recs);
+        CK(cudaGetLastError());
+    }
     // Temporaries the E-step never writes keep their initial value: the default
     // Param (1, 2) in parity mode (common.cu:57), nothing in clean mode.
     float a = mode == MC_MODE_PARITY ? 1.f : 0.f, b = mode == MC_MODE_PARITY ? 2.f : 0.f;
@@ -342,11 +416,9 @@ extern "C" int mc_model_create(int model_type, int mode, int device, mc_model** 
 extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, const int32_t* pidx,
                                const uint16_t* click, int64_t n_qd, void* stream) {
     if (!m) return set_error(MC_ERR_INVALID, "model_upload: null model");
-    if (n < 0 || n_qd < 0 || n > (int64_t)1 << 31) return set_error(MC_ERR_INVALID, "model_upload: bad sizes");
+    if (n < 0 || n_qd < 0 || n > ((int64_t)1 << 31) - 64 || n_qd >= ((int64_t)1 << 31))
+        return set_error(MC_ERR_INVALID, "model_upload: bad sizes");
     if (n > 0 && (!query || !pidx || !click)) return set_error(MC_ERR_INVALID, "model_upload: null input");
-    for (int64_t i = 0; i < n * MC_R; i++)
-        if (pidx[i] < 0 || pidx[i] >= n_qd)
-            return set_error(MC_ERR_INVALID, "model_upload: parameter index out of [0, n_qd) at " + std::to_string(i));
     CK(cudaSetDevice(m->device));
     m->free_train();
     cudaStream_t st = m->pick(stream);
@@ -354,75 +426,18 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     m->n_qd = n_qd;
     m->stride = std::max<int64_t>(32, (n + 31) / 32 * 32);
 
-    // Query segments and their qd ranges.
-    m->seg_begin.clear(); m->seg_lo.clear(); m->seg_hi.clear();
-    m->fused_ok = true;
-    for (int64_t s = 0; s < n; s++) {
-        if (s == 0 || query[s] != query[s - 1]) {
-            m->seg_begin.push_back(s);
-            m->seg_lo.push_back(INT64_MAX);
-            m->seg_hi.push_back(INT64_MIN);
-        }
-        for (int r = 0; r < MC_R; r++) {
-            int64_t p = pidx[s * MC_R + r];
-            m->seg_lo.back() = std::min(m->seg_lo.back(), p);
-            m->seg_hi.back() = std::max(m->seg_hi.back(), p + 1);
-        }
-    }
-    m->seg_begin.push_back(n);
-    for (size_t g = 1; g < m->seg_lo.size(); g++)
-        if (m->seg_lo[g] < m->seg_hi[g - 1]) {
-            m->fused_ok = false;
-            m->fused_reason = "sessions are not grouped by query with per-query contiguous parameter indices "
-                              "(as Dataset::parse_dataset leaves them)";
-            break;
-        }
-
-    // Constant parts of the statistics.
-    std::vector<uint2> cnt((size_t)std::max<int64_t>(n_qd, 1), make_uint2(0, 0));
-    std::vector<double> pconst((size_t)(2 * m->n_pub), 0.0);
-    std::vector<int64_t> w(MC_UBM_SLOTS, 0), wc(MC_UBM_SLOTS, 0), clicked_r(MC_R, 0);
-    for (int64_t s = 0; s < n; s++) {
-        unsigned mk = click[s];
-        int last = 9, slot[MC_R];
-        for (int r = 0; r < MC_R; r++) {
-            uint2& c = cnt[(size_t)pidx[s * MC_R + r]];
-            c.x++;
-            if ((mk >> r) & 1u) { c.y++; clicked_r[r]++; }
-            slot[r] = r * (r + 1) / 2 + last;
-            if ((mk >> r) & 1u) last = r;
-        }
-        if (m->model == MC_UBM)
-            for (int r = 0; r < MC_R; r++) {
-                bool alive = true;
-                for (int r2 = r + 1; r2 < MC_R; r2++) alive = alive && slot[r2] != slot[r];
-                if (alive) { w[slot[r]]++; if ((mk >> r) & 1u) wc[slot[r]]++; }
-            }
-    }
-    for (int k = 0; k < m->n_pub; k++) {
-        double num = 1.0, den = 2.0;
-        if (m->model == MC_PBM) { num += (double)clicked_r[k]; den += (double)n; }
-        if (m->model == MC_UBM) {
-            num += (double)wc[k];
-            den += (double)w[k];
-            if (m->mode == MC_MODE_PARITY) { num += (double)(n - w[k]); den += 2.0 * (double)(n - w[k]); }
-        }
-        pconst[(size_t)(2 * k)] = num;
-        pconst[(size_t)(2 * k + 1)] = den;
-    }
-
-    // Rank-major planes.
-    std::vector<int32_t> planes((size_t)(m->stride * MC_R), 0);
+    // Query segments (runs of equal query id).
+    m->seg_begin.clear();
     for (int64_t s = 0; s < n; s++)
-        for (int r = 0; r < MC_R; r++) planes[(size_t)(r * m->stride + s)] = pidx[s * MC_R + r];
-    m->h_pidx.assign(pidx, pidx + n * MC_R);
-    m->h_click.assign(click, click + n);
+        if (s == 0 || query[s] != query[s - 1]) m->seg_begin.push_back(s);
+    const int64_t n_seg = (int64_t)m->seg_begin.size();
+    m->seg_begin.push_back(n);
 
     int rc;
     int64_t& B = m->bytes;
-    if ((rc = dalloc(&m->d_pidx, planes.size(), &B))) return rc;
+    if ((rc = dalloc(&m->d_pidx, (size_t)(m->stride * MC_R), &B))) return rc;
     if ((rc = dalloc(&m->d_click, (size_t)std::max<int64_t>(n, 1), &B))) return rc;
-    if ((rc = dalloc(&m->d_cnt, cnt.size(), &B))) return rc;
+    if ((rc = dalloc(&m->d_cnt, (size_t)std::max<int64_t>(n_qd, 1), &B))) return rc;
     if ((rc = dalloc(&m->d_atr, (size_t)std::max<int64_t>(n_qd, 1), &B))) return rc;
     if (m->model == MC_DBN && (rc = dalloc(&m->d_sat, (size_t)std::max<int64_t>(n_qd, 1), &B))) return rc;
     if ((rc = dalloc(&m->d_pub_theta, 2 * MC_MAX_PUB, &B))) return rc;
@@ -433,12 +448,86 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     if ((rc = dalloc(&m->d_status, 1, &B))) return rc;
     if ((rc = dalloc(&m->d_fit, 1, &B))) return rc;
     if ((rc = dalloc(&m->d_ws, 1, &B))) return rc;
-    CK(cudaMemcpyAsync(m->d_pidx, planes.data(), planes.size() * 4, cudaMemcpyHostToDevice, st));
-    if (n) CK(cudaMemcpyAsync(m->d_click, click, (size_t)n * 2, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(m->d_cnt, cnt.data(), cnt.size() * sizeof(uint2), cudaMemcpyHostToDevice, st));
-    std::vector<float> half((size_t)std::max<int64_t>(n_qd, 2 * MC_MAX_PUB), 0.5f);
-    CK(cudaMemcpyAsync(m->d_atr, half.data(), (size_t)std::max<int64_t>(n_qd, 1) * 4, cudaMemcpyHostToDevice, st));
-    if (m->d_sat) CK(cudaMemcpyAsync(m->d_sat, half.data(), (size_t)std::max<int64_t>(n_qd, 1) * 4, cudaMemcpyHostToDevice, st));
+
+    // Scratch for the preparation pass.
+    int32_t* d_src = nullptr;
+    int64_t* d_seg_begin = nullptr;
+    int *d_seg_lo = nullptr, *d_seg_hi = nullptr, *d_flag = nullptr;
+    unsigned long long* d_pub_counts = nullptr;
+    int64_t scratch = 0;
+    auto free_scratch = [&]() { dfree(d_src); dfree(d_seg_begin); dfree(d_seg_lo); dfree(d_seg_hi); dfree(d_flag); dfree(d_pub_counts); };
+    if ((rc = dalloc(&d_src, (size_t)std::max<int64_t>(n * MC_R, 1), &scratch)) ||
+        (rc = dalloc(&d_seg_begin, (size_t)(n_seg + 1), &scratch)) ||
+        (rc = dalloc(&d_seg_lo, (size_t)std::max<int64_t>(n_seg, 1), &scratch)) ||
+        (rc = dalloc(&d_seg_hi, (size_t)std::max<int64_t>(n_seg, 1), &scratch)) ||
+        (rc = dalloc(&d_flag, 1, &scratch)) || (rc = dalloc(&d_pub_counts, 2 * MC_UBM_SLOTS, &scratch))) {
+        free_scratch();
+        return rc;
+    }
+    std::vector<int> init_lo((size_t)std::max<int64_t>(n_seg, 1), INT_MAX), init_hi((size_t)std::max<int64_t>(n_seg, 1), INT_MIN);
+    cudaError_t e = cudaSuccess;
+    auto ck = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+    if (n) {
+        ck(cudaMemcpyAsync(d_src, pidx, (size_t)n * MC_R * 4, cudaMemcpyHostToDevice, st));
+        ck(cudaMemcpyAsync(m->d_click, click, (size_t)n * 2, cudaMemcpyHostToDevice, st));
+    }
+    ck(cudaMemcpyAsync(d_seg_begin, m->seg_begin.data(), (size_t)(n_seg + 1) * 8, cudaMemcpyHostToDevice, st));
+    ck(cudaMemcpyAsync(d_seg_lo, init_lo.data(), init_lo.size() * 4, cudaMemcpyHostToDevice, st));
+    ck(cudaMemcpyAsync(d_seg_hi, init_hi.data(), init_hi.size() * 4, cudaMemcpyHostToDevice, st));
+    ck(cudaMemsetAsync(d_flag, 0, 4, st));
+    ck(cudaMemsetAsync(d_pub_counts, 0, 2 * MC_UBM_SLOTS * 8, st));
+    ck(cudaMemsetAsync(m->d_pidx, 0, (size_t)(m->stride * MC_R) * 4, st));
+    ck(cudaMemsetAsync(m->d_cnt, 0, (size_t)std::max<int64_t>(n_qd, 1) * sizeof(uint2), st));
+    if (n && e == cudaSuccess) {
+        int grid = (int)std::min<int64_t>((n + 255) / 256, (int64_t)8 * m->n_sm);
+        prep_kernel<<<grid, 256, 0, st>>>(n, m->stride, n_qd, d_src, m->d_click, d_seg_begin, n_seg, m->model,
+                                          m->d_pidx, m->d_cnt, d_seg_lo, d_seg_hi, d_pub_counts, d_flag);
+        ck(cudaGetLastError());
+    }
+    int flag = 0;
+    std::vector<unsigned long long> pub_counts(2 * MC_UBM_SLOTS, 0);
+    std::vector<int> lo(init_lo.size()), hi(init_hi.size());
+    ck(cudaMemcpyAsync(&flag, d_flag, 4, cudaMemcpyDeviceToHost, st));
+    ck(cudaMemcpyAsync(pub_counts.data(), d_pub_counts, pub_counts.size() * 8, cudaMemcpyDeviceToHost, st));
+    ck(cudaMemcpyAsync(lo.data(), d_seg_lo, lo.size() * 4, cudaMemcpyDeviceToHost, st));
+    ck(cudaMemcpyAsync(hi.data(), d_seg_hi, hi.size() * 4, cudaMemcpyDeviceToHost, st));
+    ck(cudaStreamSynchronize(st));
+    free_scratch();
+    if (e != cudaSuccess) return cuda_fail("model_upload", e);
+    if (flag) {
+        m->free_train();
+        return set_error(MC_ERR_INVALID, "model_upload: a parameter index is outside [0, n_qd)");
+    }
+
+    // Fused path precondition: per-query qd ranges disjoint and increasing.
+    m->seg_lo.assign(lo.begin(), lo.begin() + n_seg);
+    m->seg_hi.assign(hi.begin(), hi.begin() + n_seg);
+    m->fused_ok = true;
+    for (int64_t g = 1; g < n_seg; g++)
+        if (m->seg_lo[(size_t)g] < m->seg_hi[(size_t)g - 1]) {
+            m->fused_ok = false;
+            m->fused_reason = "sessions are not grouped by query with per-query contiguous parameter indices "
+                              "(as Dataset::parse_dataset leaves them)";
+            break;
+        }
+
+    // Public constants: prior plus the parts fixed by the click pattern.
+    std::vector<double> pconst((size_t)(2 * m->n_pub), 0.0);
+    for (int k = 0; k < m->n_pub; k++) {
+        double num = 1.0, den = 2.0;
+        if (m->model == MC_PBM) { num += (double)pub_counts[(size_t)k]; den += (double)n; }
+        if (m->model == MC_UBM) {
+            double w = (double)pub_counts[(size_t)k], wc = (double)pub_counts[(size_t)(MC_UBM_SLOTS + k)];
+            num += wc;
+            den += w;
+            if (m->mode == MC_MODE_PARITY) { num += (double)n - w; den += 2.0 * ((double)n - w); }
+        }
+        pconst[(size_t)(2 * k)] = num;
+        pconst[(size_t)(2 * k + 1)] = den;
+    }
+    std::vector<float> half(2 * MC_MAX_PUB, 0.5f);
+    CK(launch_fill_value(m->d_atr, std::max<int64_t>(n_qd, 1), 0.5f, st));
+    if (m->d_sat) CK(launch_fill_value(m->d_sat, std::max<int64_t>(n_qd, 1), 0.5f, st));
     CK(cudaMemcpyAsync(m->d_pub_theta, half.data(), 2 * MC_MAX_PUB * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(m->d_pub_bins, 0, (size_t)(2 * m->n_pub) * 8, st));
     CK(cudaMemcpyAsync(m->d_pub_const, pconst.data(), pconst.size() * 8, cudaMemcpyHostToDevice, st));
@@ -749,4 +838,18 @@ extern "C" void mc_model_destroy(mc_model* m) {
     m->free_train();
     if (m->own_stream) cudaStreamDestroy(m->own_stream);
     delete m;
+}
+
+extern "C" int mc_model_init_parameters(mc_model* m, void* stream) {
+    if (!m) return set_error(MC_ERR_INVALID, "init_parameters: null model");
+    if (!m->uploaded) return set_error(MC_ERR_STATE, "init_parameters: no training sessions uploaded");
+    CK(cudaSetDevice(m->device));
+    cudaStream_t st = m->pick(stream);
+    std::vector<float> half(2 * MC_MAX_PUB, 0.5f);
+    CK(launch_fill_value(m->d_atr, std::max<int64_t>(m->n_qd, 1), 0.5f, st));
+    if (m->d_sat) CK(launch_fill_value(m->d_sat, std::max<int64_t>(m->n_qd, 1), 0.5f, st));
+    CK(cudaMemcpyAsync(m->d_pub_theta, half.data(), 2 * MC_MAX_PUB * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(m->d_iter, 0, 4, st));
+    CK(cudaStreamSynchronize(st));
+    return MC_OK;
 }
