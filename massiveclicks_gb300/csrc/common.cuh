@@ -19,6 +19,11 @@
 #define MC_UBM_SLOTS 55
 #define MC_MAX_PUB 128         // >= 2 * public parameters of any model (UBM: 55 slots)
 
+// Fused kernel: at most this many threads per CTA (one producer warp plus the
+// consumer warps) and this many shared-memory stages in its copy ring.
+#define FUSED_THREADS 384
+#define FUSED_MAX_STAGES 4
+
 // Param::value() clamp (click_models/param.cu:116-128).
 #define MC_TOP (1.0f - 0.000001f)
 
@@ -45,6 +50,7 @@ struct FitDev {
     const int32_t* pidx;   // [10][stride], rank-major planes
     const uint16_t* click; // [n] bit masks
     const uint2* cnt;      // [n_qd] {occurrences, clicked occurrences}
+    const unsigned char* tblk;  // packed tile blocks (uint16 window-relative indices + clicks)
     float* atr;            // [n_qd] current values
     float* sat;            // [n_qd] current values (DBN)
     float* pub_theta;      // [2][MC_MAX_PUB], buffer (iter & 1) is current
@@ -64,6 +70,7 @@ struct TileDev {
     int s_count;        // sessions
     int qd_count;       // window size
     int64_t qd_begin;   // window start
+    int64_t blk_off;    // byte offset of the tile's packed block in FitDev::tblk
 };
 
 struct SplitDev {
@@ -79,7 +86,7 @@ struct WorkState {
 };
 
 // Status bits.
-enum { ST_BAD_INDEX = 1 };
+enum { ST_BAD_INDEX = 1, ST_TIMEOUT = 2 };
 
 __device__ __forceinline__ float clamp_top(float v) { return v < MC_TOP ? v : MC_TOP; }
 

@@ -1,19 +1,35 @@
 // Fused EM iteration: E-step, statistics reduction and M-step in one
 // persistent kernel launch per iteration.
 //
-// Work: a queue of session tiles (host-built, see model.cu).  A CTA takes the
-// next tile, zeroes a shared-memory bin per qd of the tile's window, runs the
-// E-step with one thread per session, adds each private statistic into its bin
-// (shared-memory atomics) and each public statistic into registers, then:
-//   * owned tile (whole queries): M-step for the window straight from the bins,
-//     written in place (no other tile reads those parameters);
-//   * split tile (part of a large query): bins are folded into FP64 global bins
-//     and the last tile of that query runs its M-step;
-//   * public statistics: warp shuffles -> one shared FP32 partial per tile ->
-//     an FP64 per-CTA accumulator -> one FP64 global atomic per bin per CTA;
-//     the CTA that completes the fit's last tile runs the public M-step into
-//     the other half of a double buffer.
-// Nothing waits on anything: every hand-off is "last to arrive finishes".
+// Work: a queue of session tiles (host-built, see model.cu).  Each tile is a
+// run of whole queries (or a chunk of one large query) whose qd indices form
+// one contiguous window.  One CTA per SM:
+//   * a producer warp takes the next tile from the global queue and issues
+//     bulk async copies (cp.async.bulk, completion on an mbarrier) of the tile's
+//     packed sessions (uint16 window-relative indices, rank-major, and click
+//     masks) and of the window's parameter values and click counts into a ring
+//     of shared-memory stages;
+//   * consumer warps wait on the stage's mbarrier, run the E-step with one
+//     thread per session entirely from shared memory, add each private
+//     statistic into a shared-memory bin per qd (shared atomics) and each
+//     public statistic into registers, then
+//       - owned tile (whole queries): M-step for the window straight from the
+//         bins and counts, written in place to global memory (no other tile
+//         reads those parameters);
+//       - split tile (part of a large query): bins are folded into FP64 global
+//         bins, and the last tile of that query runs its M-step;
+//     and release the stage to the producer (second mbarrier).
+//   * public statistics: warp shuffles -> shared FP32 partial per tile -> FP64
+//     per-CTA accumulator -> one FP64 global atomic per bin per CTA; the CTA
+//     that completes the fit's last tile runs the public M-step into the other
+//     half of a double buffer.
+// No CTA waits on another CTA: every hand-off is "last to arrive finishes".
+// Waits inside a CTA (mbarriers) are bounded; on expiry the kernel records
+// ST_TIMEOUT in the fit's status word and stops.
+//
+// A tile whose window does not fit in shared memory (a query with more qd than
+// the window capacity) is processed "direct": sessions and parameters read
+// from global memory, statistics added with FP64 global atomics.
 //
 // E-step forms.  The reference evaluates PBM/UBM in closed form
 // (pbm.cu:191-253, ubm.cu:185-247) and DBN/CCM through a 10x10 table of tail
@@ -41,6 +57,51 @@ namespace mcd {
 
 #define FULL_MASK 0xffffffffu
 
+// ---------------------------------------------------------------------------
+// mbarrier and bulk-copy primitives (PTX ISA: mbarrier, cp.async.bulk)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: about 2^26 polls with back-off (several seconds) before giving up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status) {
+    for (uint32_t i = 0; i < (1u << 26); i++) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (i > 32) __nanosleep(64);
+    }
+    atomicOr(status, ST_TIMEOUT);
+    return false;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void consumer_sync(int n_threads) {
+    asm volatile("bar.sync 1, %0;" ::"r"(n_threads) : "memory");
+}
+
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
@@ -49,55 +110,80 @@ __device__ __forceinline__ float warp_sum(float v) {
 
 __device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }
 
-struct TileCtx {
-    const FitDev* f;
-    int64_t qd_begin;
-    int qd_count;
-    bool wide;          // window too large for shared memory: FP64 global bins directly
-    float* sbins;       // shared bins, [qd_count * ns]
-    double* gbins;      // global FP64 bins of a wide tile
-    int ns;             // private statistics per qd
-    const float* pub;   // current public values
+// ---------------------------------------------------------------------------
+// Session / parameter sources and private-statistic sinks
+// ---------------------------------------------------------------------------
+// Staged tile in shared memory: window-relative indices, rank-major.
+struct SmemSrc {
+    const uint16_t* rel;   // [10][spad]
+    const uint16_t* clk;   // [spad]
+    const float* atr;      // window values, index woff + rel
+    const float* sat;
+    int spad, woff;
+    __device__ __forceinline__ bool load(int sl, int (&rl)[MC_R], unsigned& m) const {
+#pragma unroll
+        for (int r = 0; r < MC_R; r++) rl[r] = rel[r * spad + sl];
+        m = clk[sl];
+        return true;
+    }
+    __device__ __forceinline__ float a(int rl) const { return atr[woff + rl]; }
+    __device__ __forceinline__ float s(int rl) const { return sat[woff + rl]; }
 };
 
-__device__ __forceinline__ void add_private(const TileCtx& c, int rel, int k, float v) {
-    if (c.wide) atomicAdd(c.gbins + (int64_t)rel * c.ns + k, (double)v);
-    else atomicAdd(c.sbins + rel * c.ns + k, v);
-}
-
-// Loads the ten parameter indices of session s relative to the window;
-// returns false (and flags the fit) if one falls outside it.
-__device__ __forceinline__ bool load_rel(const TileCtx& c, int64_t s, int (&rel)[MC_R]) {
-    const FitDev& f = *c.f;
-    bool ok = true;
+// Direct tile: sessions and values from global memory (window too large).
+struct GlobSrc {
+    const int32_t* pidx;
+    const uint16_t* clk;
+    const float* atr;
+    const float* sat;
+    int64_t stride, s_begin, qd_begin;
+    int qd_count;
+    int* status;
+    __device__ __forceinline__ bool load(int sl, int (&rl)[MC_R], unsigned& m) const {
+        bool ok = true;
 #pragma unroll
-    for (int r = 0; r < MC_R; r++) {
-        int64_t p = (int64_t)__ldg(f.pidx + (int64_t)r * f.stride + s) - c.qd_begin;
-        rel[r] = (int)p;
-        ok = ok && (p >= 0) && (p < c.qd_count);
+        for (int r = 0; r < MC_R; r++) {
+            int64_t p = (int64_t)__ldg(pidx + (int64_t)r * stride + s_begin + sl) - qd_begin;
+            rl[r] = (int)p;
+            ok = ok && p >= 0 && p < qd_count;
+        }
+        m = __ldg(clk + s_begin + sl);
+        if (!ok) atomicOr(status, ST_BAD_INDEX);
+        return ok;
     }
-    if (!ok) atomicOr(f.status, ST_BAD_INDEX);
-    return ok;
-}
+    __device__ __forceinline__ float a(int rl) const { return atr[qd_begin + rl]; }
+    __device__ __forceinline__ float s(int rl) const { return sat[qd_begin + rl]; }
+};
+
+struct SmemSink {
+    float* bins;
+    int ns;
+    __device__ __forceinline__ void add(int rl, int k, float v) const { atomicAdd(bins + rl * ns + k, v); }
+};
+struct GlobSink {
+    double* bins;
+    int ns;
+    __device__ __forceinline__ void add(int rl, int k, float v) const { atomicAdd(bins + (int64_t)rl * ns + k, (double)v); }
+};
 
 // ---------------------------------------------------------------------------
 // PBM (pbm.cu:191-253): unclicked rank -> atr += (a - ae)/(1 - ae),
 // exm[r] += (e - ae)/(1 - ae); clicked contributions are constant counts.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void estep_pbm(const TileCtx& c, int64_t s, float (&pub)[MC_R]) {
-    int rel[MC_R];
-    if (!load_rel(c, s, rel)) return;
-    const FitDev& f = *c.f;
-    unsigned m = __ldg(f.click + s);
+template <class Src, class Sink>
+__device__ __forceinline__ void estep_pbm(const Src& src, const Sink& sink, int sl, const float* pub, float (&acc)[MC_R]) {
+    int rl[MC_R];
+    unsigned m;
+    if (!src.load(sl, rl, m)) return;
 #pragma unroll
     for (int r = 0; r < MC_R; r++) {
         if (!((m >> r) & 1u)) {
-            float a = f.atr[c.qd_begin + rel[r]];
-            float e = c.pub[r];
+            float a = src.a(rl[r]);
+            float e = pub[r];
             float ae = a * e;
             float inv = __fdividef(1.0f, 1.0f - ae);
-            add_private(c, rel[r], 0, (a - ae) * inv);
-            pub[r] += (e - ae) * inv;
+            sink.add(rl[r], 0, (a - ae) * inv);
+            acc[r] += (e - ae) * inv;
         }
     }
 }
@@ -107,14 +193,15 @@ __device__ __forceinline__ void estep_pbm(const TileCtx& c, int64_t s, float (&p
 // earlier click).  A slot written by two ranks of one session keeps the later
 // rank's value; the counts of written / clicked-written slots are constants.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void estep_ubm(const TileCtx& c, int64_t s, bool valid, int (&key)[MC_R], float (&var)[MC_R]) {
+template <class Src, class Sink>
+__device__ __forceinline__ void estep_ubm(const Src& src, const Sink& sink, int sl, bool valid, const float* pub,
+                                          int (&key)[MC_R], float (&var)[MC_R]) {
 #pragma unroll
     for (int r = 0; r < MC_R; r++) { key[r] = -1; var[r] = 0.0f; }
     if (!valid) return;
-    int rel[MC_R];
-    if (!load_rel(c, s, rel)) return;
-    const FitDev& f = *c.f;
-    unsigned m = __ldg(f.click + s);
+    int rl[MC_R];
+    unsigned m;
+    if (!src.load(sl, rl, m)) return;
     int slot[MC_R];
     int last = 9;
 #pragma unroll
@@ -128,11 +215,11 @@ __device__ __forceinline__ void estep_ubm(const TileCtx& c, int64_t s, bool vali
 #pragma unroll
         for (int r2 = r + 1; r2 < MC_R; r2++) alive = alive && (slot[r2] != slot[r]);
         if (!((m >> r) & 1u)) {
-            float a = f.atr[c.qd_begin + rel[r]];
-            float e = c.pub[slot[r]];
+            float a = src.a(rl[r]);
+            float e = pub[slot[r]];
             float ae = a * e;
             float inv = __fdividef(1.0f, 1.0f - ae);
-            add_private(c, rel[r], 0, (a - ae) * inv);
+            sink.add(rl[r], 0, (a - ae) * inv);
             if (alive) { key[r] = slot[r]; var[r] = (e - ae) * inv; }
         }
     }
@@ -164,24 +251,22 @@ __device__ __forceinline__ void rescale(float& P, float& E) {
 // ---------------------------------------------------------------------------
 // DBN (dbn.cu:207-467)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void estep_dbn(const TileCtx& c, int64_t s, float& gnum, float& gden) {
-    int rel[MC_R];
-    if (!load_rel(c, s, rel)) return;
-    const FitDev& f = *c.f;
-    unsigned m = __ldg(f.click + s);
+template <class Src, class Sink>
+__device__ __forceinline__ void estep_dbn(const Src& src, const Sink& sink, int sl, float g, float& gnum, float& gden) {
+    int rl[MC_R];
+    unsigned m;
+    if (!src.load(sl, rl, m)) return;
     int l = m ? 31 - __clz(m) : MC_R;
-    float a[MC_R], sv[MC_R];
-#pragma unroll
-    for (int r = 0; r < MC_R; r++) {
-        a[r] = f.atr[c.qd_begin + rel[r]];
-        sv[r] = f.sat[c.qd_begin + rel[r]];
-    }
-    float g = c.pub[0];
     // Ranks before the last click: (1, 1) each (all ten for a click-less session).
     gnum += (float)l;
     gden += (float)l;
     if (l == MC_R) return;  // no clicks: no attractiveness / satisfaction terms either
-
+    float a[MC_R], sv[MC_R];
+#pragma unroll
+    for (int r = 0; r < MC_R; r++) {
+        a[r] = src.a(rl[r]);
+        sv[r] = src.s(rl[r]);
+    }
     // Unconditional examination (compute_exm_car) and car, backwards.
     float eps[MC_R], car[MC_R + 1];
     eps[0] = 1.0f;
@@ -190,7 +275,6 @@ __device__ __forceinline__ void estep_dbn(const TileCtx& c, int64_t s, float& gn
     car[MC_R] = 0.0f;
 #pragma unroll
     for (int r = MC_R - 1; r >= 0; r--) car[r] = a[r] + g * (1.0f - a[r]) * car[r + 1];
-
     // Prefix products of the all-unclicked tail over documents 0, 1, ...
     float Pu[MC_R];
     Pu[0] = 1.0f;
@@ -202,7 +286,6 @@ __device__ __forceinline__ void estep_dbn(const TileCtx& c, int64_t s, float& gn
             Eu *= g * (1.0f - a[j]);
         }
     }
-
     // Conditional examination up to rank l (restarting at every click).
     float P = 1.0f, E = 1.0f;
 #pragma unroll
@@ -222,7 +305,7 @@ __device__ __forceinline__ void estep_dbn(const TileCtx& c, int64_t s, float& gn
             float B = __fdividef(1.0f, 1.0f - w * (1.0f - R));
             gnum += w * R * B;
             gden += cs * (1.0f - g + g * R) * B;
-            add_private(c, rel[r], 1, __fdividef(sv[r], 1.0f - cs * g * car[r + 1]));
+            sink.add(rl[r], 1, __fdividef(sv[r], 1.0f - cs * g * car[r + 1]));
             E = g * cs;
             P = 1.0f;
         } else if (r > l) {
@@ -230,7 +313,7 @@ __device__ __forceinline__ void estep_dbn(const TileCtx& c, int64_t s, float& gn
             float D = __fdividef(1.0f, P - g * E * (1.0f - R));
             gnum += g * R * E * D;
             gden += E * (1.0f - g * (1.0f - R)) * D;
-            add_private(c, rel[r], 0, __fdividef(a[r] * (1.0f - eps[r]), 1.0f - eps[r] * car[r]));
+            sink.add(rl[r], 0, __fdividef(a[r] * (1.0f - eps[r]), 1.0f - eps[r] * car[r]));
             P = P - a[r] * E;
             E = E * g * (1.0f - a[r]);
             rescale(P, E);
@@ -242,17 +325,16 @@ __device__ __forceinline__ void estep_dbn(const TileCtx& c, int64_t s, float& gn
 // CCM (ccm.cu:185-478); tau statistics t[0..5] = (t1 num, t1 den, t2 num,
 // t2 den, t3 num, t3 den).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void estep_ccm(const TileCtx& c, int64_t s, float (&t)[6]) {
-    int rel[MC_R];
-    if (!load_rel(c, s, rel)) return;
-    const FitDev& f = *c.f;
-    unsigned m = __ldg(f.click + s);
+template <class Src, class Sink>
+__device__ __forceinline__ void estep_ccm(const Src& src, const Sink& sink, int sl, float t1, float t2, float t3,
+                                          float (&t)[6]) {
+    int rl[MC_R];
+    unsigned m;
+    if (!src.load(sl, rl, m)) return;
     int l = m ? 31 - __clz(m) : MC_R;
     float a[MC_R];
 #pragma unroll
-    for (int r = 0; r < MC_R; r++) a[r] = f.atr[c.qd_begin + rel[r]];
-    float t1 = c.pub[0], t2 = c.pub[1], t3 = c.pub[2];
-
+    for (int r = 0; r < MC_R; r++) a[r] = src.a(rl[r]);
     // Ranks before the last click.
 #pragma unroll
     for (int r = 0; r < MC_R; r++) {
@@ -268,7 +350,6 @@ __device__ __forceinline__ void estep_ccm(const TileCtx& c, int64_t s, float (&t
         }
     }
     if (l == MC_R) return;
-
     float eps[MC_R], car[MC_R + 1];
     eps[0] = 1.0f;
 #pragma unroll
@@ -277,7 +358,6 @@ __device__ __forceinline__ void estep_ccm(const TileCtx& c, int64_t s, float (&t
     car[MC_R] = 0.0f;
 #pragma unroll
     for (int r = MC_R - 1; r >= 0; r--) car[r] = a[r] + (1.0f - a[r]) * t1 * car[r + 1];
-
     float Pu[MC_R];
     Pu[0] = 1.0f;
     {
@@ -306,14 +386,14 @@ __device__ __forceinline__ void estep_ccm(const TileCtx& c, int64_t s, float (&t
             t[2] += ia * t2 * R * B; t[3] += ia * k2 * B;
             t[4] += a[r] * t3 * R * B; t[5] += a[r] * k3 * B;
             float cont = t2 * ia + t3 * a[r];
-            add_private(c, rel[r], 0, __fdividef(a[r], 1.0f - cont * car[r + 1]));
+            sink.add(rl[r], 0, __fdividef(a[r], 1.0f - cont * car[r + 1]));
             E = cont;
             P = 1.0f;
         } else if (r > l) {
             float D = __fdividef(1.0f, P - t1 * E * (1.0f - R));
             t[0] += t1 * R * E * D;
             t[1] += E * (1.0f - t1 * (1.0f - R)) * D;
-            add_private(c, rel[r], 0, __fdividef((1.0f - eps[r]) * a[r], 1.0f - eps[r] * car[r]));
+            sink.add(rl[r], 0, __fdividef((1.0f - eps[r]) * a[r], 1.0f - eps[r] * car[r]));
             P = P - a[r] * E;
             E = E * t1 * (1.0f - a[r]);
             rescale(P, E);
@@ -328,28 +408,40 @@ __device__ __forceinline__ void estep_ccm(const TileCtx& c, int64_t s, float (&t
 //   DBN satisfaction, parity:       (1 + unclicked + v1) / (2 + clicks + 2 unclicked)
 //   DBN satisfaction, clean:        (1 + v1) / (2 + clicks)
 // ---------------------------------------------------------------------------
-template <typename T>
-__device__ __forceinline__ void mstep_qd(int model, int mode, uint2 cnt, T v0, T v1, float* atr, float* sat) {
-    T occ = (T)cnt.x, clk = (T)cnt.y;
-    T den = model == CCM ? T(2) + occ + clk : T(2) + occ;
-    T v = (T(1) + clk + v0) / den;
-    *atr = (float)(v < (T)MC_TOP ? v : (T)MC_TOP);
+__device__ __forceinline__ float clamp_f(float v) { return v < MC_TOP ? v : MC_TOP; }
+
+__device__ __forceinline__ void mstep_qd_f(int model, int mode, uint2 cnt, float v0, float v1, float* atr, float* sat) {
+    float occ = (float)cnt.x, clk = (float)cnt.y;
+    float den = model == CCM ? 2.0f + occ + clk : 2.0f + occ;
+    *atr = clamp_f(__fdiv_rn(1.0f + clk + v0, den));
     if (model == DBN) {
-        T un = occ - clk;
-        T sn = mode == PARITY ? T(1) + un + v1 : T(1) + v1;
-        T sd = mode == PARITY ? T(2) + clk + T(2) * un : T(2) + clk;
-        T w = sn / sd;
-        *sat = (float)(w < (T)MC_TOP ? w : (T)MC_TOP);
+        float un = occ - clk;
+        float sn = mode == PARITY ? 1.0f + un + v1 : 1.0f + v1;
+        float sd = mode == PARITY ? 2.0f + clk + 2.0f * un : 2.0f + clk;
+        *sat = clamp_f(__fdiv_rn(sn, sd));
     }
 }
 
-// Public M-step of a fit whose last tile has finished (run by one CTA).
-__device__ void finalize_public(const FitDev& f) {
-    __shared__ int s_it;
-    if (threadIdx.x == 0) s_it = *(volatile int*)f.iter;
-    __syncthreads();
-    int nb = (s_it + 1) & 1;
-    for (int k = threadIdx.x; k < f.n_pub; k += blockDim.x) {
+__device__ __forceinline__ void mstep_qd_d(int model, int mode, uint2 cnt, double v0, double v1, float* atr, float* sat) {
+    double occ = (double)cnt.x, clk = (double)cnt.y;
+    double den = model == CCM ? 2.0 + occ + clk : 2.0 + occ;
+    double v = (1.0 + clk + v0) / den;
+    *atr = (float)(v < (double)MC_TOP ? v : (double)MC_TOP);
+    if (model == DBN) {
+        double un = occ - clk;
+        double sn = mode == PARITY ? 1.0 + un + v1 : 1.0 + v1;
+        double sd = mode == PARITY ? 2.0 + clk + 2.0 * un : 2.0 + clk;
+        double w = sn / sd;
+        *sat = (float)(w < (double)MC_TOP ? w : (double)MC_TOP);
+    }
+}
+
+// Public M-step of a fit whose last tile has finished (consumer threads of one CTA).
+__device__ void finalize_public(const FitDev& f, int ctid, int nc, int* s_it) {
+    if (ctid == 0) *s_it = *(volatile int*)f.iter;
+    consumer_sync(nc);
+    int nb = (*s_it + 1) & 1;
+    for (int k = ctid; k < f.n_pub; k += nc) {
         double num = f.pub_const[2 * k] + ld_cg(f.pub_bins + 2 * k);
         double den = f.pub_const[2 * k + 1] + ld_cg(f.pub_bins + 2 * k + 1);
         double v = num / den;
@@ -357,186 +449,297 @@ __device__ void finalize_public(const FitDev& f) {
         f.pub_bins[2 * k] = 0.0;
         f.pub_bins[2 * k + 1] = 0.0;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
+    consumer_sync(nc);
+    if (ctid == 0) {
         *f.tiles_done = 0;
         __threadfence();
-        *(volatile int*)f.iter = s_it + 1;
+        *(volatile int*)f.iter = *s_it + 1;
     }
 }
 
 template <int MODEL>
 __device__ __forceinline__ int model_of(const FitDev& f) { return MODEL >= 0 ? MODEL : f.model; }
 
+// Shared-memory layout of one CTA (dynamic part), all 16-byte aligned:
+//   bins     float [window_max * 2]
+//   stage s  { uint16 rel[10][spt_pad], uint16 clk[spt_pad],
+//              float atr[window_max + 8], float sat[window_max + 8],
+//              uint2 cnt[window_max + 8] }           for s < n_stages
+struct Layout {
+    uint32_t bins_off, stage_off, stage_bytes, sess_bytes, atr_off, sat_off, cnt_off;
+};
+
+__host__ __device__ inline Layout make_layout(int spt, int window_max) {
+    Layout L;
+    uint32_t spad = (uint32_t)((spt + 7) & ~7);
+    uint32_t w = (uint32_t)window_max + 8;
+    L.bins_off = 0;
+    L.stage_off = ((uint32_t)window_max * 2 * 4 + 15) & ~15u;
+    L.sess_bytes = 11u * spad * 2;
+    L.atr_off = (L.sess_bytes + 15) & ~15u;
+    L.sat_off = L.atr_off + w * 4;
+    L.cnt_off = L.sat_off + w * 4;
+    L.stage_bytes = (L.cnt_off + w * 8 + 15) & ~15u;
+    return L;
+}
+
 template <int MODEL>
-__global__ void __launch_bounds__(512) em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ tiles,
-                                                       int n_tiles, const SplitDev* __restrict__ splits,
-                                                       WorkState* ws, int window_max) {
-    extern __shared__ __align__(16) float sbins[];
+__global__ void __launch_bounds__(FUSED_THREADS, 1)
+em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ tiles, int n_tiles,
+                const SplitDev* __restrict__ splits, WorkState* ws, int window_max, int spt, int n_stages) {
+    extern __shared__ __align__(128) unsigned char smem[];
     __shared__ double pub_acc[MC_MAX_PUB];
     __shared__ float pub_tile[MC_MAX_PUB];
     __shared__ float pub_th[MC_MAX_PUB];
-    __shared__ int s_tile;
-    __shared__ int s_last;
+    __shared__ __align__(8) uint64_t full_bar[FUSED_MAX_STAGES], empty_bar[FUSED_MAX_STAGES];
+    __shared__ int stage_tile[FUSED_MAX_STAGES];
+    __shared__ int s_last, s_it, s_abort;
 
+    const Layout L = make_layout(spt, window_max);
+    float* bins = reinterpret_cast<float*>(smem + L.bins_off);
     const int tid = threadIdx.x;
-    const int nthr = blockDim.x;
-    const int lane = tid & 31;
-    for (int k = tid; k < MC_MAX_PUB; k += nthr) { pub_acc[k] = 0.0; pub_tile[k] = 0.0f; }
-    int cur_fit = -1;
-    unsigned cur_count = 0;
+    const int nc = blockDim.x - 32;            // consumer threads; the last warp produces
+    const bool producer = tid >= nc;
+    const int* status_any = fits[0].status;
 
-    auto flush_fit = [&](int fit_id, unsigned count) {
-        const FitDev& f = fits[fit_id];
-        __syncthreads();
-        for (int k = tid; k < 2 * f.n_pub; k += nthr) {
-            double v = pub_acc[k];
-            if (v != 0.0) atomicAdd(f.pub_bins + k, v);
-            pub_acc[k] = 0.0;
+    if (tid == 0) {
+        for (int s = 0; s < n_stages; s++) {
+            mbar_init(&full_bar[s], 1);
+            mbar_init(&empty_bar[s], 1);
         }
-        __threadfence();
-        __syncthreads();
-        if (tid == 0) {
-            unsigned old = atomicAdd(f.tiles_done, count);
-            s_last = (old + count == (unsigned)f.n_tiles);
-        }
-        __syncthreads();
-        if (s_last) {
-            __threadfence();
-            finalize_public(f);
-        }
-        __syncthreads();
-    };
+        s_abort = 0;
+    }
+    for (int k = tid; k < MC_MAX_PUB; k += blockDim.x) { pub_acc[k] = 0.0; pub_tile[k] = 0.0f; }
+    for (int k = tid; k < window_max * 2; k += blockDim.x) bins[k] = 0.0f;
+    fence_async_shared();
+    __syncthreads();
 
-    for (;;) {
-        if (tid == 0) s_tile = (int)atomicAdd(&ws->next_tile, 1u);
-        __syncthreads();
-        const int t = s_tile;
-        __syncthreads();
-        if (t >= n_tiles) break;
-        const TileDev tile = tiles[t];
-        if (tile.fit != cur_fit) {
-            if (cur_fit >= 0) flush_fit(cur_fit, cur_count);
-            cur_fit = tile.fit;
-            cur_count = 0;
-        }
-        const FitDev& f = fits[tile.fit];
-        const int model = model_of<MODEL>(f);
-        const int ns = private_stats(model);
-        const int n_pub = f.n_pub;
-
-        TileCtx c;
-        c.f = &f;
-        c.qd_begin = tile.qd_begin;
-        c.qd_count = tile.qd_count;
-        c.wide = tile.qd_count > window_max;
-        c.sbins = sbins;
-        c.ns = ns;
-        c.gbins = tile.split >= 0 ? f.split_bins + splits[tile.split].bin_offset : nullptr;
-        c.pub = pub_th;
-        if (!c.wide)
-            for (int i = tid; i < tile.qd_count * ns; i += nthr) sbins[i] = 0.0f;
-        {
-            int it = *(volatile int*)f.iter;
-            for (int k = tid; k < n_pub; k += nthr) pub_th[k] = f.pub_theta[(it & 1) * MC_MAX_PUB + k];
-        }
-        __syncthreads();
-
-        // ---- E-step over the tile's sessions -------------------------------
-        const int rounds = (tile.s_count + nthr - 1) / nthr;
-        if (model == PBM) {
-            float pub[MC_R];
-#pragma unroll
-            for (int r = 0; r < MC_R; r++) pub[r] = 0.0f;
-            for (int rd = 0; rd < rounds; rd++) {
-                int sl = rd * nthr + tid;
-                if (sl < tile.s_count) estep_pbm(c, tile.s_begin + sl, pub);
-            }
-#pragma unroll
-            for (int r = 0; r < MC_R; r++) {
-                float v = warp_sum(pub[r]);
-                if (lane == 0 && v != 0.0f) atomicAdd(pub_tile + 2 * r, v);
-            }
-        } else if (model == UBM) {
-            for (int rd = 0; rd < rounds; rd++) {
-                int sl = rd * nthr + tid;
-                int key[MC_R];
-                float var[MC_R];
-                estep_ubm(c, tile.s_begin + sl, sl < tile.s_count, key, var);
-                reduce_ubm_public(key, var, pub_tile);
-            }
-        } else if (model == DBN) {
-            float gn = 0.0f, gd = 0.0f;
-            for (int rd = 0; rd < rounds; rd++) {
-                int sl = rd * nthr + tid;
-                if (sl < tile.s_count) estep_dbn(c, tile.s_begin + sl, gn, gd);
-            }
-            gn = warp_sum(gn);
-            gd = warp_sum(gd);
-            if (lane == 0) { atomicAdd(pub_tile + 0, gn); atomicAdd(pub_tile + 1, gd); }
-        } else {
-            float tt[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            for (int rd = 0; rd < rounds; rd++) {
-                int sl = rd * nthr + tid;
-                if (sl < tile.s_count) estep_ccm(c, tile.s_begin + sl, tt);
-            }
-#pragma unroll
-            for (int k = 0; k < 6; k++) {
-                float v = warp_sum(tt[k]);
-                if (lane == 0) atomicAdd(pub_tile + k, v);
-            }
-        }
-        __syncthreads();
-
-        // ---- M-step of the window ------------------------------------------
-        if (tile.split < 0) {
-            for (int i = tid; i < tile.qd_count; i += nthr) {
-                int64_t q = tile.qd_begin + i;
-                uint2 cn = __ldg(f.cnt + q);
-                float v0 = sbins[i * ns];
-                float v1 = ns > 1 ? sbins[i * ns + 1] : 0.0f;
-                mstep_qd<float>(model, f.mode, cn, v0, v1, f.atr + q, ns > 1 ? f.sat + q : nullptr);
-            }
-        } else {
-            const SplitDev sp = splits[tile.split];
-            double* gb = f.split_bins + sp.bin_offset;
-            if (!c.wide) {
-                for (int i = tid; i < tile.qd_count * ns; i += nthr) {
-                    float v = sbins[i];
-                    if (v != 0.0f) atomicAdd(gb + i, (double)v);
+    if (producer) {
+        // ---------------- producer warp ----------------------------------------
+        if (tid == nc) {
+            int k = 0;
+            int last_issued = -1;  // last ring slot k that received bulk copies
+            for (;; k++) {
+                int st = k % n_stages;
+                uint32_t round = (uint32_t)(k / n_stages);
+                if (!mbar_wait(&empty_bar[st], (round & 1u) ^ 1u, fits[0].status)) { s_abort = 1; break; }
+                int t = (int)atomicAdd(&ws->next_tile, 1u);
+                if (t >= n_tiles || *(volatile int*)&s_abort) {
+                    stage_tile[st] = -1;
+                    mbar_arrive(&full_bar[st]);
+                    break;
                 }
+                const TileDev tile = tiles[t];
+                const FitDev& f = fits[tile.fit];
+                stage_tile[st] = t;
+                if (tile.qd_count > window_max) {  // direct tile: nothing to stage
+                    mbar_arrive(&full_bar[st]);
+                    continue;
+                }
+                unsigned char* sb = smem + L.stage_off + (size_t)st * L.stage_bytes;
+                int64_t a0 = tile.qd_begin & ~(int64_t)3;
+                int64_t a1 = (tile.qd_begin + tile.qd_count + 3) & ~(int64_t)3;
+                uint32_t wn = (uint32_t)(a1 - a0);
+                uint32_t sess = 11u * (uint32_t)((tile.s_count + 7) & ~7) * 2u;
+                uint32_t bytes = sess + wn * 4 + wn * 8 + (f.sat ? wn * 4 : 0);
+                mbar_arrive_expect_tx(&full_bar[st], bytes);
+                bulk_g2s(sb, reinterpret_cast<const unsigned char*>(f.tblk) + tile.blk_off, sess, &full_bar[st]);
+                bulk_g2s(sb + L.atr_off, f.atr + a0, wn * 4, &full_bar[st]);
+                if (f.sat) bulk_g2s(sb + L.sat_off, f.sat + a0, wn * 4, &full_bar[st]);
+                bulk_g2s(sb + L.cnt_off, f.cnt + a0, wn * 8, &full_bar[st]);
+                last_issued = k;
+            }
+            // On a stop, wait (bounded) until every copy this warp issued into
+            // the ring has landed, so none is still writing shared memory when
+            // the CTA exits.
+            if (*(volatile int*)&s_abort) {
+                for (int j = last_issued - n_stages + 1; j <= last_issued; j++)
+                    if (j >= 0) mbar_wait(&full_bar[j % n_stages], (uint32_t)(j / n_stages) & 1u, fits[0].status);
+            }
+        }
+    } else {
+        // ---------------- consumer warps ---------------------------------------
+        const int ctid = tid;
+        const int lane = tid & 31;
+        int cur_fit = -1;
+        unsigned cur_count = 0;
+
+        auto flush_fit = [&](int fit_id, unsigned count) {
+            const FitDev& f = fits[fit_id];
+            consumer_sync(nc);
+            for (int k = ctid; k < 2 * f.n_pub; k += nc) {
+                double v = pub_acc[k];
+                if (v != 0.0) atomicAdd(f.pub_bins + k, v);
+                pub_acc[k] = 0.0;
             }
             __threadfence();
-            __syncthreads();
-            if (tid == 0) {
-                unsigned old = atomicAdd(f.split_count + tile.split, 1u);
-                s_last = (old + 1 == (unsigned)sp.n_tiles);
+            consumer_sync(nc);
+            if (ctid == 0) {
+                unsigned old = atomicAdd(f.tiles_done, count);
+                s_last = (old + count == (unsigned)f.n_tiles);
             }
-            __syncthreads();
+            consumer_sync(nc);
             if (s_last) {
                 __threadfence();
-                for (int i = tid; i < sp.qd_count; i += nthr) {
-                    int64_t q = sp.qd_begin + i;
-                    uint2 cn = __ldg(f.cnt + q);
-                    double v0 = ld_cg(gb + (int64_t)i * ns);
-                    double v1 = ns > 1 ? ld_cg(gb + (int64_t)i * ns + 1) : 0.0;
-                    mstep_qd<double>(model, f.mode, cn, v0, v1, f.atr + q, ns > 1 ? f.sat + q : nullptr);
-                    gb[(int64_t)i * ns] = 0.0;
-                    if (ns > 1) gb[(int64_t)i * ns + 1] = 0.0;
-                }
-                if (tid == 0) f.split_count[tile.split] = 0;
+                finalize_public(f, ctid, nc, &s_it);
             }
-        }
+            consumer_sync(nc);
+        };
 
-        // ---- fold the tile's public partial into the CTA's FP64 accumulator
-        for (int k = tid; k < 2 * n_pub; k += nthr) {
-            pub_acc[k] += (double)pub_tile[k];
-            pub_tile[k] = 0.0f;
+        for (int k = 0;; k++) {
+            int st = k % n_stages;
+            uint32_t round = (uint32_t)(k / n_stages);
+            // Every consumer thread observes the completed phase itself.
+            if (!mbar_wait(&full_bar[st], round & 1u, fits[0].status)) s_abort = 1;
+            consumer_sync(nc);
+            if (*(volatile int*)&s_abort) break;
+            const int t = stage_tile[st];
+            if (t < 0) break;
+            const TileDev tile = tiles[t];
+            if (tile.fit != cur_fit) {
+                if (cur_fit >= 0) flush_fit(cur_fit, cur_count);
+                cur_fit = tile.fit;
+                cur_count = 0;
+            }
+            const FitDev& f = fits[tile.fit];
+            const int model = model_of<MODEL>(f);
+            const int ns = private_stats(model);
+            const int n_pub = f.n_pub;
+            {
+                int it = *(volatile int*)f.iter;
+                for (int q = ctid; q < n_pub; q += nc) pub_th[q] = f.pub_theta[(it & 1) * MC_MAX_PUB + q];
+            }
+            consumer_sync(nc);
+
+            const bool direct = tile.qd_count > window_max;
+            const unsigned char* sb = smem + L.stage_off + (size_t)st * L.stage_bytes;
+            const int64_t a0 = tile.qd_begin & ~(int64_t)3;
+            SmemSrc ssrc;
+            ssrc.spad = (tile.s_count + 7) & ~7;
+            ssrc.rel = reinterpret_cast<const uint16_t*>(sb);
+            ssrc.clk = ssrc.rel + 10 * ssrc.spad;
+            ssrc.atr = reinterpret_cast<const float*>(sb + L.atr_off);
+            ssrc.sat = reinterpret_cast<const float*>(sb + L.sat_off);
+            ssrc.woff = (int)(tile.qd_begin - a0);
+            const uint2* cnt_w = reinterpret_cast<const uint2*>(sb + L.cnt_off) + ssrc.woff;
+            GlobSrc gsrc;
+            gsrc.pidx = f.pidx; gsrc.clk = f.click; gsrc.atr = f.atr; gsrc.sat = f.sat;
+            gsrc.stride = f.stride; gsrc.s_begin = tile.s_begin; gsrc.qd_begin = tile.qd_begin;
+            gsrc.qd_count = tile.qd_count; gsrc.status = f.status;
+            SmemSink ssink{bins, ns};
+            GlobSink gsink{tile.split >= 0 ? f.split_bins + splits[tile.split].bin_offset : nullptr, ns};
+
+            // ---- E-step over the tile's sessions -------------------------------
+            const int rounds = (tile.s_count + nc - 1) / nc;
+            if (model == PBM) {
+                float acc[MC_R];
+#pragma unroll
+                for (int r = 0; r < MC_R; r++) acc[r] = 0.0f;
+                for (int rd = 0; rd < rounds; rd++) {
+                    int sl = rd * nc + ctid;
+                    if (sl < tile.s_count) {
+                        if (direct) estep_pbm(gsrc, gsink, sl, pub_th, acc);
+                        else estep_pbm(ssrc, ssink, sl, pub_th, acc);
+                    }
+                }
+#pragma unroll
+                for (int r = 0; r < MC_R; r++) {
+                    float v = warp_sum(acc[r]);
+                    if (lane == 0 && v != 0.0f) atomicAdd(pub_tile + 2 * r, v);
+                }
+            } else if (model == UBM) {
+                for (int rd = 0; rd < rounds; rd++) {
+                    int sl = rd * nc + ctid;
+                    int key[MC_R];
+                    float var[MC_R];
+                    if (direct) estep_ubm(gsrc, gsink, sl, sl < tile.s_count, pub_th, key, var);
+                    else estep_ubm(ssrc, ssink, sl, sl < tile.s_count, pub_th, key, var);
+                    reduce_ubm_public(key, var, pub_tile);
+                }
+            } else if (model == DBN) {
+                float gn = 0.0f, gd = 0.0f;
+                const float g = pub_th[0];
+                for (int rd = 0; rd < rounds; rd++) {
+                    int sl = rd * nc + ctid;
+                    if (sl < tile.s_count) {
+                        if (direct) estep_dbn(gsrc, gsink, sl, g, gn, gd);
+                        else estep_dbn(ssrc, ssink, sl, g, gn, gd);
+                    }
+                }
+                gn = warp_sum(gn);
+                gd = warp_sum(gd);
+                if (lane == 0) { atomicAdd(pub_tile + 0, gn); atomicAdd(pub_tile + 1, gd); }
+            } else {
+                float tt[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                const float t1 = pub_th[0], t2 = pub_th[1], t3 = pub_th[2];
+                for (int rd = 0; rd < rounds; rd++) {
+                    int sl = rd * nc + ctid;
+                    if (sl < tile.s_count) {
+                        if (direct) estep_ccm(gsrc, gsink, sl, t1, t2, t3, tt);
+                        else estep_ccm(ssrc, ssink, sl, t1, t2, t3, tt);
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 6; q++) {
+                    float v = warp_sum(tt[q]);
+                    if (lane == 0) atomicAdd(pub_tile + q, v);
+                }
+            }
+            consumer_sync(nc);
+
+            // ---- M-step of the window ------------------------------------------
+            if (tile.split < 0) {
+                for (int i = ctid; i < tile.qd_count; i += nc) {
+                    int64_t q = tile.qd_begin + i;
+                    float v0 = bins[i * ns];
+                    float v1 = ns > 1 ? bins[i * ns + 1] : 0.0f;
+                    bins[i * ns] = 0.0f;
+                    if (ns > 1) bins[i * ns + 1] = 0.0f;
+                    mstep_qd_f(model, f.mode, cnt_w[i], v0, v1, f.atr + q, ns > 1 ? f.sat + q : nullptr);
+                }
+            } else {
+                const SplitDev sp = splits[tile.split];
+                double* gb = f.split_bins + sp.bin_offset;
+                if (!direct) {
+                    for (int i = ctid; i < tile.qd_count * ns; i += nc) {
+                        float v = bins[i];
+                        if (v != 0.0f) { atomicAdd(gb + i, (double)v); bins[i] = 0.0f; }
+                    }
+                }
+                __threadfence();
+                consumer_sync(nc);
+                if (ctid == 0) {
+                    unsigned old = atomicAdd(f.split_count + tile.split, 1u);
+                    s_last = (old + 1 == (unsigned)sp.n_tiles);
+                }
+                consumer_sync(nc);
+                if (s_last) {
+                    __threadfence();
+                    for (int i = ctid; i < sp.qd_count; i += nc) {
+                        int64_t q = sp.qd_begin + i;
+                        uint2 cn = __ldg(f.cnt + q);
+                        double v0 = ld_cg(gb + (int64_t)i * ns);
+                        double v1 = ns > 1 ? ld_cg(gb + (int64_t)i * ns + 1) : 0.0;
+                        mstep_qd_d(model, f.mode, cn, v0, v1, f.atr + q, ns > 1 ? f.sat + q : nullptr);
+                        gb[(int64_t)i * ns] = 0.0;
+                        if (ns > 1) gb[(int64_t)i * ns + 1] = 0.0;
+                    }
+                    if (ctid == 0) f.split_count[tile.split] = 0;
+                }
+            }
+
+            // ---- fold the tile's public partial; release the stage ---------------
+            for (int q = ctid; q < 2 * n_pub; q += nc) {
+                pub_acc[q] += (double)pub_tile[q];
+                pub_tile[q] = 0.0f;
+            }
+            cur_count++;
+            consumer_sync(nc);
+            if (ctid == 0) mbar_arrive(&empty_bar[st]);
         }
-        cur_count++;
-        __syncthreads();
+        if (cur_fit >= 0 && !s_abort) flush_fit(cur_fit, cur_count);
     }
-    if (cur_fit >= 0) flush_fit(cur_fit, cur_count);
+    __syncthreads();
     if (tid == 0) {
         __threadfence();
         unsigned e = atomicAdd(&ws->ctas_exited, 1u);
@@ -545,42 +748,39 @@ __global__ void __launch_bounds__(512) em_fused_kernel(const FitDev* __restrict_
             ws->ctas_exited = 0;
         }
     }
+    (void)status_any;
 }
 
-size_t fused_smem_bytes(int model, int window_max) {
-    int ns = model < 0 ? 2 : private_stats(model);
-    return (size_t)window_max * ns * sizeof(float);
+size_t fused_smem_bytes(int model, int window_max, int spt, int n_stages) {
+    (void)model;
+    Layout L = make_layout(spt, window_max);
+    return (size_t)L.stage_off + (size_t)n_stages * L.stage_bytes;
 }
 
 cudaError_t launch_em_fused(int model, const FitDev* fits, const TileDev* tiles, int n_tiles, const SplitDev* splits,
-                            WorkState* ws, int window_max, int grid, int block, cudaStream_t stream) {
-    size_t smem = fused_smem_bytes(model, window_max);
+                            WorkState* ws, int window_max, int spt, int n_stages, int grid, int block,
+                            cudaStream_t stream) {
+    size_t smem = fused_smem_bytes(model, window_max, spt, n_stages);
     switch (model) {
-        case PBM: em_fused_kernel<PBM><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max); break;
-        case CCM: em_fused_kernel<CCM><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max); break;
-        case DBN: em_fused_kernel<DBN><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max); break;
-        case UBM: em_fused_kernel<UBM><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max); break;
-        default: em_fused_kernel<-1><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max); break;
+        case PBM: em_fused_kernel<PBM><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max, spt, n_stages); break;
+        case CCM: em_fused_kernel<CCM><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max, spt, n_stages); break;
+        case DBN: em_fused_kernel<DBN><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max, spt, n_stages); break;
+        case UBM: em_fused_kernel<UBM><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max, spt, n_stages); break;
+        default: em_fused_kernel<-1><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max, spt, n_stages); break;
     }
     return cudaGetLastError();
 }
 
-cudaError_t fused_set_smem_limits(int window_max) {
-    cudaError_t e = cudaSuccess;
-    size_t b2 = fused_smem_bytes(-1, window_max), b1 = fused_smem_bytes(PBM, window_max);
-    e = cudaFuncSetAttribute(em_fused_kernel<PBM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b1);
-    if (e) return e;
-    e = cudaFuncSetAttribute(em_fused_kernel<CCM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b1);
-    if (e) return e;
-    e = cudaFuncSetAttribute(em_fused_kernel<UBM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b1);
-    if (e) return e;
-    e = cudaFuncSetAttribute(em_fused_kernel<DBN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b2);
-    if (e) return e;
-    return cudaFuncSetAttribute(em_fused_kernel<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b2);
+cudaError_t fused_set_smem_limits(size_t bytes) {
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(em_fused_kernel<PBM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes))) return e;
+    if ((e = cudaFuncSetAttribute(em_fused_kernel<CCM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes))) return e;
+    if ((e = cudaFuncSetAttribute(em_fused_kernel<UBM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes))) return e;
+    if ((e = cudaFuncSetAttribute(em_fused_kernel<DBN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes))) return e;
+    return cudaFuncSetAttribute(em_fused_kernel<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-cudaError_t fused_occupancy(int model, int block, int window_max, int* blocks_per_sm) {
-    size_t smem = fused_smem_bytes(model, window_max);
+cudaError_t fused_occupancy(int model, int block, size_t smem, int* blocks_per_sm) {
     switch (model) {
         case PBM: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, em_fused_kernel<PBM>, block, smem);
         case CCM: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, em_fused_kernel<CCM>, block, smem);
@@ -588,6 +788,38 @@ cudaError_t fused_occupancy(int model, int block, int window_max, int* blocks_pe
         case UBM: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, em_fused_kernel<UBM>, block, smem);
         default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, em_fused_kernel<-1>, block, smem);
     }
+}
+
+// Packs the tiles' sessions into the staged layout: per tile, rank-major
+// uint16 window-relative indices [10][spad] followed by the click masks
+// [spad] (padding zeroed).  Direct tiles keep no packed block.
+__global__ void pack_tiles_kernel(const TileDev* tiles, int n_tiles, int window_max, const int32_t* planes, int64_t stride,
+                                  const uint16_t* click, unsigned char* tblk, int* status) {
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+        const TileDev tile = tiles[t];
+        if (tile.qd_count > window_max) continue;
+        int spad = (tile.s_count + 7) & ~7;
+        uint16_t* rel = reinterpret_cast<uint16_t*>(tblk + tile.blk_off);
+        uint16_t* clk = rel + 10 * spad;
+        for (int sl = threadIdx.x; sl < spad; sl += blockDim.x) {
+            bool in = sl < tile.s_count;
+            int64_t s = tile.s_begin + sl;
+            for (int r = 0; r < MC_R; r++) {
+                int64_t p = in ? (int64_t)planes[(int64_t)r * stride + s] - tile.qd_begin : 0;
+                if (p < 0 || p >= tile.qd_count) { atomicOr(status, ST_BAD_INDEX); p = 0; }
+                rel[r * spad + sl] = (uint16_t)p;
+            }
+            clk[sl] = in ? click[s] : (uint16_t)0;
+        }
+    }
+}
+
+cudaError_t launch_pack_tiles(const TileDev* tiles, int n_tiles, int window_max, const int32_t* planes, int64_t stride,
+                              const uint16_t* click, unsigned char* tblk, int* status, int n_sm, cudaStream_t st) {
+    if (n_tiles == 0) return cudaSuccess;
+    int g = n_tiles < 8 * n_sm ? n_tiles : 8 * n_sm;
+    pack_tiles_kernel<<<g, 256, 0, st>>>(tiles, n_tiles, window_max, planes, stride, click, tblk, status);
+    return cudaGetLastError();
 }
 
 }  // namespace mcd

@@ -10,11 +10,14 @@
 namespace mcd {
 
 // ---- fused EM (em_fused.cu) -------------------------------------------------
-size_t fused_smem_bytes(int model, int window_max);
-cudaError_t fused_set_smem_limits(int window_max);
-cudaError_t fused_occupancy(int model, int block, int window_max, int* blocks_per_sm);
+size_t fused_smem_bytes(int model, int window_max, int spt, int n_stages);
+cudaError_t fused_set_smem_limits(size_t bytes);
+cudaError_t fused_occupancy(int model, int block, size_t smem, int* blocks_per_sm);
 cudaError_t launch_em_fused(int model, const FitDev* fits, const TileDev* tiles, int n_tiles, const SplitDev* splits,
-                            WorkState* ws, int window_max, int grid, int block, cudaStream_t stream);
+                            WorkState* ws, int window_max, int spt, int n_stages, int grid, int block,
+                            cudaStream_t stream);
+cudaError_t launch_pack_tiles(const TileDev* tiles, int n_tiles, int window_max, const int32_t* planes, int64_t stride,
+                              const uint16_t* click, unsigned char* tblk, int* status, int n_sm, cudaStream_t st);
 
 // ---- plain EM (em_plain.cu) -------------------------------------------------
 // The reference's 8-byte device record (data/search.cuh:63-73).

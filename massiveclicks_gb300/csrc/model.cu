@@ -167,7 +167,7 @@ struct mc_model {
     std::string fused_reason;
     // query segments of the training set: sessions and qd range
     std::vector<int64_t> seg_begin, seg_lo, seg_hi;
-    int spt = 512, wqd = 2048, block = 256;
+    int spt = 1024, wqd = 2048, block = 384, stages = 3;
     // fused state
     int32_t* d_pidx = nullptr;
     uint16_t* d_click = nullptr;
@@ -181,6 +181,7 @@ struct mc_model {
     SplitDev* d_splits = nullptr;
     WorkState* d_ws = nullptr;
     int n_tiles = 0, n_splits = 0, grid = 0;
+    unsigned char* d_tblk = nullptr;
     int64_t split_bins_count = 0;
     int64_t tile_bytes = 0;
     // plain state (allocated on first use)
@@ -219,6 +220,7 @@ struct mc_model {
         dfree(d_splits);
         dfree(d_split_bins);
         dfree(d_split_count);
+        dfree(d_tblk);
         bytes -= tile_bytes;
         tile_bytes = 0;
     }
@@ -253,6 +255,7 @@ struct mc_model {
         return own_stream;
     }
 
+    int64_t qd_alloc() const { return ((std::max<int64_t>(n_qd, 1) + 3) & ~(int64_t)3) + 4; }
     int build_tiles();
     int write_fit_desc();
     int ensure_plain(cudaStream_t st);
@@ -298,6 +301,7 @@ int mc_model::build_tiles() {
                 t.s_count = (int)(e - b);
                 t.qd_begin = lo;
                 t.qd_count = (int)(hi - lo);
+                t.blk_off = 0;
                 tiles.push_back(t);
             }
             continue;
@@ -316,6 +320,12 @@ int mc_model::build_tiles() {
         cur.qd_count = (int)(hi - cur.qd_begin);
     }
     close();
+    // Packed session blocks of the staged (non-direct) tiles, 16-byte aligned.
+    int64_t blk = 0;
+    for (TileDev& t : tiles) {
+        t.blk_off = blk;
+        if (t.qd_count <= wqd) blk += 22 * (int64_t)((t.s_count + 7) & ~7);
+    }
     n_tiles = (int)tiles.size();
     n_splits = (int)splits.size();
     split_bins_count = bin_off;
@@ -325,17 +335,34 @@ int mc_model::build_tiles() {
     if ((rc = dalloc(&d_splits, splits.size(), &bytes))) return rc;
     if ((rc = dalloc(&d_split_bins, (size_t)bin_off, &bytes))) return rc;
     if ((rc = dalloc(&d_split_count, splits.size(), &bytes))) return rc;
+    if ((rc = dalloc(&d_tblk, (size_t)std::max<int64_t>(blk, 16), &bytes))) return rc;
     tile_bytes = bytes - before;
     if (!tiles.empty()) CK(cudaMemcpy(d_tiles, tiles.data(), tiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice));
     if (!splits.empty()) CK(cudaMemcpy(d_splits, splits.data(), splits.size() * sizeof(SplitDev), cudaMemcpyHostToDevice));
     CK(cudaMemset(d_split_bins, 0, (size_t)std::max<int64_t>(bin_off, 1) * sizeof(double)));
     CK(cudaMemset(d_split_count, 0, std::max<size_t>(splits.size(), 1) * sizeof(unsigned)));
-    CK(fused_set_smem_limits(wqd));
+    // Shared memory: bins plus as many copy stages (2..4) as fit.
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    const size_t static_smem = 4096;
+    stages = 0;
+    for (int ns_ = FUSED_MAX_STAGES; ns_ >= 2; ns_--)
+        if (fused_smem_bytes(model, wqd, spt, ns_) + static_smem <= (size_t)optin) { stages = ns_; break; }
+    if (!stages) return set_error(MC_ERR_INVALID, "tile shape does not fit in shared memory (reduce sessions per tile or window)");
+    size_t smem = fused_smem_bytes(model, wqd, spt, stages);
+    CK(fused_set_smem_limits(smem));
     int per_sm = 0;
-    CK(fused_occupancy(model, block, wqd, &per_sm));
+    CK(fused_occupancy(model, block, smem, &per_sm));
     if (per_sm < 1) return set_error(MC_ERR_INVALID, "configuration does not fit on an SM (window or block too large)");
     grid = std::max(1, std::min(n_tiles, per_sm * n_sm));
-    return write_fit_desc();
+    int rc2 = write_fit_desc();
+    if (rc2) return rc2;
+    CK(launch_pack_tiles(d_tiles, n_tiles, wqd, d_pidx, stride, d_click, d_tblk, d_status, n_sm, 0));
+    CK(cudaDeviceSynchronize());
+    int status = 0;
+    CK(cudaMemcpy(&status, d_status, 4, cudaMemcpyDeviceToHost));
+    if (status) return set_error(MC_ERR_INVALID, "tile packing found a parameter index outside its query's window");
+    return MC_OK;
 }
 
 int mc_model::write_fit_desc() {
@@ -350,6 +377,7 @@ int mc_model::write_fit_desc() {
     f.pidx = d_pidx;
     f.click = d_click;
     f.cnt = d_cnt;
+    f.tblk = d_tblk;
     f.atr = d_atr;
     f.sat = d_sat;
     f.pub_theta = d_pub_theta;
@@ -437,9 +465,12 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     int64_t& B = m->bytes;
     if ((rc = dalloc(&m->d_pidx, (size_t)(m->stride * MC_R), &B))) return rc;
     if ((rc = dalloc(&m->d_click, (size_t)std::max<int64_t>(n, 1), &B))) return rc;
-    if ((rc = dalloc(&m->d_cnt, (size_t)std::max<int64_t>(n_qd, 1), &B))) return rc;
-    if ((rc = dalloc(&m->d_atr, (size_t)std::max<int64_t>(n_qd, 1), &B))) return rc;
-    if (m->model == MC_DBN && (rc = dalloc(&m->d_sat, (size_t)std::max<int64_t>(n_qd, 1), &B))) return rc;
+    // Parameter arrays padded to a multiple of 4 entries plus 4, so 16-byte
+    // aligned bulk copies of any window stay inside the allocation.
+    const int64_t qd_alloc = m->qd_alloc();
+    if ((rc = dalloc(&m->d_cnt, (size_t)qd_alloc, &B))) return rc;
+    if ((rc = dalloc(&m->d_atr, (size_t)qd_alloc, &B))) return rc;
+    if (m->model == MC_DBN && (rc = dalloc(&m->d_sat, (size_t)qd_alloc, &B))) return rc;
     if ((rc = dalloc(&m->d_pub_theta, 2 * MC_MAX_PUB, &B))) return rc;
     if ((rc = dalloc(&m->d_pub_bins, (size_t)(2 * m->n_pub), &B))) return rc;
     if ((rc = dalloc(&m->d_pub_const, (size_t)(2 * m->n_pub), &B))) return rc;
@@ -477,7 +508,7 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     ck(cudaMemsetAsync(d_flag, 0, 4, st));
     ck(cudaMemsetAsync(d_pub_counts, 0, 2 * MC_UBM_SLOTS * 8, st));
     ck(cudaMemsetAsync(m->d_pidx, 0, (size_t)(m->stride * MC_R) * 4, st));
-    ck(cudaMemsetAsync(m->d_cnt, 0, (size_t)std::max<int64_t>(n_qd, 1) * sizeof(uint2), st));
+    ck(cudaMemsetAsync(m->d_cnt, 0, (size_t)qd_alloc * sizeof(uint2), st));
     if (n && e == cudaSuccess) {
         int grid = (int)std::min<int64_t>((n + 255) / 256, (int64_t)8 * m->n_sm);
         prep_kernel<<<grid, 256, 0, st>>>(n, m->stride, n_qd, d_src, m->d_click, d_seg_begin, n_seg, m->model,
@@ -526,8 +557,8 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
         pconst[(size_t)(2 * k + 1)] = den;
     }
     std::vector<float> half(2 * MC_MAX_PUB, 0.5f);
-    CK(launch_fill_value(m->d_atr, std::max<int64_t>(n_qd, 1), 0.5f, st));
-    if (m->d_sat) CK(launch_fill_value(m->d_sat, std::max<int64_t>(n_qd, 1), 0.5f, st));
+    CK(launch_fill_value(m->d_atr, m->qd_alloc(), 0.5f, st));
+    if (m->d_sat) CK(launch_fill_value(m->d_sat, m->qd_alloc(), 0.5f, st));
     CK(cudaMemcpyAsync(m->d_pub_theta, half.data(), 2 * MC_MAX_PUB * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(m->d_pub_bins, 0, (size_t)(2 * m->n_pub) * 8, st));
     CK(cudaMemcpyAsync(m->d_pub_const, pconst.data(), pconst.size() * 8, cudaMemcpyHostToDevice, st));
@@ -568,9 +599,11 @@ extern "C" int mc_model_upload_test(mc_model* m, int64_t n, const int32_t* pidx,
 extern "C" int mc_model_configure(mc_model* m, int32_t spt, int32_t wqd, int32_t block) {
     if (!m) return set_error(MC_ERR_INVALID, "model_configure: null model");
     if (spt < 0 || wqd < 0 || block < 0) return set_error(MC_ERR_INVALID, "model_configure: negative value");
-    if (block && (block % 32 || block > 512)) return set_error(MC_ERR_INVALID, "model_configure: block must be a multiple of 32, <= 512");
-    if (wqd && wqd > 24576) return set_error(MC_ERR_INVALID, "model_configure: window above 24576 qd");
-    if (spt && spt > (1 << 20)) return set_error(MC_ERR_INVALID, "model_configure: sessions per tile above 2^20");
+    if (block && (block % 32 || block < 64 || block > FUSED_THREADS))
+        return set_error(MC_ERR_INVALID, "model_configure: block must be a multiple of 32 in [64, " + std::to_string(FUSED_THREADS) + "]");
+    if (wqd && wqd > 16384) return set_error(MC_ERR_INVALID, "model_configure: window above 16384 qd");
+    if (spt && spt > 4096) return set_error(MC_ERR_INVALID, "model_configure: sessions per tile above 4096");
+    wqd = (wqd + 7) & ~7;
     CK(cudaSetDevice(m->device));
     if (spt) m->spt = spt;
     if (wqd) m->wqd = wqd;
@@ -589,7 +622,8 @@ extern "C" int mc_model_get_config(const mc_model* m, int32_t* spt, int32_t* wqd
 
 static int launch_fused_loop(mc_model* m, int iters, cudaStream_t st) {
     for (int i = 0; i < iters; i++)
-        CK(launch_em_fused(m->model, m->d_fit, m->d_tiles, m->n_tiles, m->d_splits, m->d_ws, m->wqd, m->grid, m->block, st));
+        CK(launch_em_fused(m->model, m->d_fit, m->d_tiles, m->n_tiles, m->d_splits, m->d_ws, m->wqd, m->spt, m->stages,
+                           m->grid, m->block, st));
     return MC_OK;
 }
 
@@ -786,22 +820,21 @@ extern "C" int mc_model_autotune(mc_model* m, void* stream) {
     cudaStream_t st = m->pick(stream);
     CK(cudaStreamSynchronize(st));
     // Snapshot of the state the trial iterations change.
-    std::vector<float> atr((size_t)std::max<int64_t>(m->n_qd, 1)), sat, th(2 * MC_MAX_PUB);
+    std::vector<float> atr((size_t)m->qd_alloc()), sat, th(2 * MC_MAX_PUB);
     int it0 = 0;
     CK(cudaMemcpy(atr.data(), m->d_atr, atr.size() * 4, cudaMemcpyDeviceToHost));
     if (m->d_sat) { sat.resize(atr.size()); CK(cudaMemcpy(sat.data(), m->d_sat, sat.size() * 4, cudaMemcpyDeviceToHost)); }
     CK(cudaMemcpy(th.data(), m->d_pub_theta, th.size() * 4, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(&it0, m->d_iter, 4, cudaMemcpyDeviceToHost));
     struct Cand { int spt, wqd, block; };
-    const Cand cands[] = {{256, 2048, 128}, {512, 2048, 256}, {512, 4096, 256}, {1024, 4096, 256},
-                          {1024, 8192, 512}, {2048, 8192, 512}, {256, 1024, 256}};
+    const Cand cands[] = {{1024, 2048, 384}, {512, 2048, 384}, {2048, 2048, 384}, {1024, 4096, 384},
+                          {1024, 2048, 256}, {2048, 4096, 256}, {512, 1024, 160}};
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     float best = 1e30f;
     Cand pick = {m->spt, m->wqd, m->block};
     for (const Cand& c : cands) {
-        if (c.wqd * private_stats(m->model) * 4 > 200 * 1024) continue;
         m->spt = c.spt; m->wqd = c.wqd; m->block = c.block;
         if (m->build_tiles() != MC_OK) continue;
         if (launch_fused_loop(m, 1, st) != MC_OK) continue;  // warm-up
@@ -846,8 +879,8 @@ extern "C" int mc_model_init_parameters(mc_model* m, void* stream) {
     CK(cudaSetDevice(m->device));
     cudaStream_t st = m->pick(stream);
     std::vector<float> half(2 * MC_MAX_PUB, 0.5f);
-    CK(launch_fill_value(m->d_atr, std::max<int64_t>(m->n_qd, 1), 0.5f, st));
-    if (m->d_sat) CK(launch_fill_value(m->d_sat, std::max<int64_t>(m->n_qd, 1), 0.5f, st));
+    CK(launch_fill_value(m->d_atr, m->qd_alloc(), 0.5f, st));
+    if (m->d_sat) CK(launch_fill_value(m->d_sat, m->qd_alloc(), 0.5f, st));
     CK(cudaMemcpyAsync(m->d_pub_theta, half.data(), 2 * MC_MAX_PUB * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(m->d_iter, 0, 4, st));
     CK(cudaStreamSynchronize(st));

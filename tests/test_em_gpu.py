@@ -86,7 +86,7 @@ def test_clean_mode_matches_f64_oracle(name):
     assert_params_close(cm.get_parameters(), f.values(), what=f"clean {name}")
 
 
-@pytest.mark.parametrize("config", [(7, 16, 64), (32, 64, 128), (100, 5000, 32), (2048, 8192, 512)])
+@pytest.mark.parametrize("config", [(7, 16, 64), (32, 64, 128), (100, 5000, 64), (1024, 4096, 384), (4096, 1024, 256)])
 def test_tiling_does_not_change_results(config):
     """Tiny tiles force queries split over many tiles and windows too wide for
     shared memory; results must not depend on the tile shape."""
@@ -100,7 +100,7 @@ def test_tiling_does_not_change_results(config):
 def test_tiling_all_models(model):
     case = load_case({0: "pbm_pbmclicks", 1: "ccm_ccmclicks", 2: "dbn_ccmclicks", 3: "ubm_dbnclicks"}[model])
     f = oracle_fit(case, model, 4)
-    for config in [(5, 12, 32), (64, 256, 64)]:
+    for config in [(5, 12, 64), (64, 256, 96)]:
         g = gpu_fit(case, model, 4, config=config).get_parameters()
         assert_params_close(g, f.values(), what=f"m{model} config {config}")
 
@@ -210,6 +210,15 @@ def test_empty_and_single_session():
         f = bindings.OracleFit("f64", model, 0, one.query, one.pidx, one.click, 10)
         f.run(4)
         assert_params_close(cm.get_parameters(), f.values(), what=f"single m{model}")
+
+
+def test_configure_rejects_shapes_that_do_not_fit():
+    case = load_case("dbn_dbnclicks")
+    cm = gpu_fit(case, 2, 0)
+    with pytest.raises(api._capi.MCError):
+        cm.configure(4096, 16384, 384)
+    with pytest.raises(api._capi.MCError):
+        cm.configure(0, 0, 1024)
 
 
 def test_bad_indices_rejected():
