@@ -71,6 +71,8 @@ struct TileDev {
     int qd_count;       // window size
     int64_t qd_begin;   // window start
     int64_t blk_off;    // byte offset of the tile's packed block in FitDev::tblk
+    int s_packed;       // sessions in the packed block (see pack_tiles_kernel)
+    int pad_;
 };
 
 struct SplitDev {
@@ -84,6 +86,11 @@ struct WorkState {
     unsigned next_tile;
     unsigned ctas_exited;
 };
+
+// Counters of the upload pass beyond the UBM slot counts.
+#define MC_PUB_COUNTS 128
+#define MC_CNT_DBN_BEFORE_LAST 120   // DBN: sum over sessions of the last-click rank (10 if none)
+#define MC_CNT_CCM_UNCLICKED_BEFORE_LAST 121  // CCM: unclicked ranks before the last click (10 if none)
 
 // Status bits.
 enum { ST_BAD_INDEX = 1, ST_TIMEOUT = 2 };

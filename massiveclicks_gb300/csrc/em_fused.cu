@@ -257,10 +257,10 @@ __device__ __forceinline__ void estep_dbn(const Src& src, const Sink& sink, int 
     unsigned m;
     if (!src.load(sl, rl, m)) return;
     int l = m ? 31 - __clz(m) : MC_R;
-    // Ranks before the last click: (1, 1) each (all ten for a click-less session).
-    gnum += (float)l;
-    gden += (float)l;
-    if (l == MC_R) return;  // no clicks: no attractiveness / satisfaction terms either
+    // Ranks before the last click contribute exactly (1, 1) each, a session
+    // without clicks (10, 10) and nothing else: constants of the fit, added to
+    // the public M-step at upload (model.cu), so they are skipped here.
+    if (l == MC_R) return;
     float a[MC_R], sv[MC_R];
 #pragma unroll
     for (int r = 0; r < MC_R; r++) {
@@ -339,13 +339,13 @@ __device__ __forceinline__ void estep_ccm(const Src& src, const Sink& sink, int 
 #pragma unroll
     for (int r = 0; r < MC_R; r++) {
         if (r < l) {
+            // An unclicked rank before the last click adds exactly (1, 1) to
+            // tau_1: a constant of the fit, added at upload (model.cu).
             if ((m >> r) & 1u) {
                 float x = (1.0f - a[r]) * t2, y = a[r] * t3;
                 float u = __fdividef(x, x + y);
                 t[2] += u; t[3] += u;
                 t[4] += 1.0f - u; t[5] += 1.0f - u;
-            } else {
-                t[0] += 1.0f; t[1] += 1.0f;
             }
         }
     }
@@ -540,10 +540,10 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
                 int64_t a0 = tile.qd_begin & ~(int64_t)3;
                 int64_t a1 = (tile.qd_begin + tile.qd_count + 3) & ~(int64_t)3;
                 uint32_t wn = (uint32_t)(a1 - a0);
-                uint32_t sess = 11u * (uint32_t)((tile.s_count + 7) & ~7) * 2u;
+                uint32_t sess = 11u * (uint32_t)((tile.s_packed + 7) & ~7) * 2u;
                 uint32_t bytes = sess + wn * 4 + wn * 8 + (f.sat ? wn * 4 : 0);
                 mbar_arrive_expect_tx(&full_bar[st], bytes);
-                bulk_g2s(sb, reinterpret_cast<const unsigned char*>(f.tblk) + tile.blk_off, sess, &full_bar[st]);
+                if (sess) bulk_g2s(sb, reinterpret_cast<const unsigned char*>(f.tblk) + tile.blk_off, sess, &full_bar[st]);
                 bulk_g2s(sb + L.atr_off, f.atr + a0, wn * 4, &full_bar[st]);
                 if (f.sat) bulk_g2s(sb + L.sat_off, f.sat + a0, wn * 4, &full_bar[st]);
                 bulk_g2s(sb + L.cnt_off, f.cnt + a0, wn * 8, &full_bar[st]);
@@ -615,7 +615,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             const unsigned char* sb = smem + L.stage_off + (size_t)st * L.stage_bytes;
             const int64_t a0 = tile.qd_begin & ~(int64_t)3;
             SmemSrc ssrc;
-            ssrc.spad = (tile.s_count + 7) & ~7;
+            ssrc.spad = (tile.s_packed + 7) & ~7;
             ssrc.rel = reinterpret_cast<const uint16_t*>(sb);
             ssrc.clk = ssrc.rel + 10 * ssrc.spad;
             ssrc.atr = reinterpret_cast<const float*>(sb + L.atr_off);
@@ -630,14 +630,17 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             GlobSink gsink{tile.split >= 0 ? f.split_bins + splits[tile.split].bin_offset : nullptr, ns};
 
             // ---- E-step over the tile's sessions -------------------------------
-            const int rounds = (tile.s_count + nc - 1) / nc;
+            // Staged tiles hold only the sessions that carry variable statistics
+            // (pack_tiles_kernel); direct tiles read every session.
+            const int n_sess = direct ? tile.s_count : tile.s_packed;
+            const int rounds = (n_sess + nc - 1) / nc;
             if (model == PBM) {
                 float acc[MC_R];
 #pragma unroll
                 for (int r = 0; r < MC_R; r++) acc[r] = 0.0f;
                 for (int rd = 0; rd < rounds; rd++) {
                     int sl = rd * nc + ctid;
-                    if (sl < tile.s_count) {
+                    if (sl < n_sess) {
                         if (direct) estep_pbm(gsrc, gsink, sl, pub_th, acc);
                         else estep_pbm(ssrc, ssink, sl, pub_th, acc);
                     }
@@ -652,8 +655,8 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
                     int sl = rd * nc + ctid;
                     int key[MC_R];
                     float var[MC_R];
-                    if (direct) estep_ubm(gsrc, gsink, sl, sl < tile.s_count, pub_th, key, var);
-                    else estep_ubm(ssrc, ssink, sl, sl < tile.s_count, pub_th, key, var);
+                    if (direct) estep_ubm(gsrc, gsink, sl, sl < n_sess, pub_th, key, var);
+                    else estep_ubm(ssrc, ssink, sl, sl < n_sess, pub_th, key, var);
                     reduce_ubm_public(key, var, pub_tile);
                 }
             } else if (model == DBN) {
@@ -661,7 +664,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
                 const float g = pub_th[0];
                 for (int rd = 0; rd < rounds; rd++) {
                     int sl = rd * nc + ctid;
-                    if (sl < tile.s_count) {
+                    if (sl < n_sess) {
                         if (direct) estep_dbn(gsrc, gsink, sl, g, gn, gd);
                         else estep_dbn(ssrc, ssink, sl, g, gn, gd);
                     }
@@ -674,7 +677,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
                 const float t1 = pub_th[0], t2 = pub_th[1], t3 = pub_th[2];
                 for (int rd = 0; rd < rounds; rd++) {
                     int sl = rd * nc + ctid;
-                    if (sl < tile.s_count) {
+                    if (sl < n_sess) {
                         if (direct) estep_ccm(gsrc, gsink, sl, t1, t2, t3, tt);
                         else estep_ccm(ssrc, ssink, sl, t1, t2, t3, tt);
                     }
@@ -792,33 +795,78 @@ cudaError_t fused_occupancy(int model, int block, size_t smem, int* blocks_per_s
 
 // Packs the tiles' sessions into the staged layout: per tile, rank-major
 // uint16 window-relative indices [10][spad] followed by the click masks
-// [spad] (padding zeroed).  Direct tiles keep no packed block.
-__global__ void pack_tiles_kernel(const TileDev* tiles, int n_tiles, int window_max, const int32_t* planes, int64_t stride,
-                                  const uint16_t* click, unsigned char* tblk, int* status) {
+// [spad] (padding zeroed), spad = s_packed rounded up to 8.  Sessions are
+// ordered by click pattern (DBN/CCM: last-click rank; PBM/UBM: click mask), a
+// stable bitonic sort on (key, position), so the lanes of a warp take the
+// same branches.  DBN and CCM sessions without clicks carry no variable
+// statistic (their constant contributions are folded in at upload) and are
+// left out; s_packed records how many sessions remain.  Direct tiles keep no
+// packed block.
+__global__ void pack_tiles_kernel(int model, TileDev* tiles, int n_tiles, int window_max, const int32_t* planes,
+                                  int64_t stride, const uint16_t* click, unsigned char* tblk, int* status) {
+    extern __shared__ uint32_t keys[];
+    __shared__ int s_kept;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
         const TileDev tile = tiles[t];
         if (tile.qd_count > window_max) continue;
-        int spad = (tile.s_count + 7) & ~7;
+        const bool drop_clickless = model == DBN || model == CCM;
+        int P = 1;
+        while (P < tile.s_count) P <<= 1;
+        for (int i = threadIdx.x; i < P; i += blockDim.x) {
+            uint32_t key = 0xFFFFFFFFu;
+            if (i < tile.s_count) {
+                unsigned m = click[tile.s_begin + i];
+                uint32_t k16 = drop_clickless ? (m ? (uint32_t)(31 - __clz(m)) : 0xFFFFu) : m;
+                key = (k16 << 16) | (uint32_t)i;
+            }
+            keys[i] = key;
+        }
+        __syncthreads();
+        for (int k = 2; k <= P; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                    int ixj = i ^ j;
+                    if (ixj > i) {
+                        uint32_t x = keys[i], y = keys[ixj];
+                        bool up = (i & k) == 0;
+                        if ((x > y) == up) { keys[i] = y; keys[ixj] = x; }
+                    }
+                }
+                __syncthreads();
+            }
+        int kept = 0;
+        for (int i = threadIdx.x; i < tile.s_count; i += blockDim.x) kept += (keys[i] >> 16) != 0xFFFFu;
+        if (threadIdx.x == 0) s_kept = 0;
+        __syncthreads();
+        atomicAdd(&s_kept, kept);
+        __syncthreads();
+        const int n_kept = s_kept;
+        const int spad = (n_kept + 7) & ~7;
         uint16_t* rel = reinterpret_cast<uint16_t*>(tblk + tile.blk_off);
         uint16_t* clk = rel + 10 * spad;
-        for (int sl = threadIdx.x; sl < spad; sl += blockDim.x) {
-            bool in = sl < tile.s_count;
-            int64_t s = tile.s_begin + sl;
+        for (int i = threadIdx.x; i < spad; i += blockDim.x) {
+            bool in = i < n_kept;
+            int64_t s = tile.s_begin + (in ? (int64_t)(keys[i] & 0xFFFFu) : 0);
             for (int r = 0; r < MC_R; r++) {
                 int64_t p = in ? (int64_t)planes[(int64_t)r * stride + s] - tile.qd_begin : 0;
                 if (p < 0 || p >= tile.qd_count) { atomicOr(status, ST_BAD_INDEX); p = 0; }
-                rel[r * spad + sl] = (uint16_t)p;
+                rel[r * spad + i] = (uint16_t)p;
             }
-            clk[sl] = in ? click[s] : (uint16_t)0;
+            clk[i] = in ? click[s] : (uint16_t)0;
         }
+        if (threadIdx.x == 0) tiles[t].s_packed = n_kept;
+        __syncthreads();
     }
 }
 
-cudaError_t launch_pack_tiles(const TileDev* tiles, int n_tiles, int window_max, const int32_t* planes, int64_t stride,
-                              const uint16_t* click, unsigned char* tblk, int* status, int n_sm, cudaStream_t st) {
+cudaError_t launch_pack_tiles(int model, TileDev* tiles, int n_tiles, int window_max, int spt, const int32_t* planes,
+                              int64_t stride, const uint16_t* click, unsigned char* tblk, int* status, int n_sm,
+                              cudaStream_t st) {
     if (n_tiles == 0) return cudaSuccess;
+    int P = 1;
+    while (P < spt) P <<= 1;
     int g = n_tiles < 8 * n_sm ? n_tiles : 8 * n_sm;
-    pack_tiles_kernel<<<g, 256, 0, st>>>(tiles, n_tiles, window_max, planes, stride, click, tblk, status);
+    pack_tiles_kernel<<<g, 256, (size_t)P * 4, st>>>(model, tiles, n_tiles, window_max, planes, stride, click, tblk, status);
     return cudaGetLastError();
 }
 

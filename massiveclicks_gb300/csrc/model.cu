@@ -79,8 +79,8 @@ __global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32
                             const uint16_t* __restrict__ click, const int64_t* __restrict__ seg_begin, int64_t n_seg,
                             int model, int32_t* planes, uint2* cnt, int* seg_lo, int* seg_hi,
                             unsigned long long* pub_counts, int* flag) {
-    __shared__ unsigned int sc[2 * MC_UBM_SLOTS];
-    for (int k = threadIdx.x; k < 2 * MC_UBM_SLOTS; k += blockDim.x) sc[k] = 0;
+    __shared__ unsigned int sc[MC_PUB_COUNTS];
+    for (int k = threadIdx.x; k < MC_PUB_COUNTS; k += blockDim.x) sc[k] = 0;
     __syncthreads();
     const int64_t step = (int64_t)gridDim.x * blockDim.x;
     const int64_t base = (int64_t)blockIdx.x * blockDim.x;
@@ -112,6 +112,9 @@ __global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32
                 if (c) last = r;
                 if (model == 0 && c) atomicAdd(&sc[r], 1u);
             }
+            int lc = m ? 31 - __clz(m) : MC_R;
+            if (model == 2) atomicAdd(&sc[MC_CNT_DBN_BEFORE_LAST], (unsigned)lc);
+            if (model == 1) atomicAdd(&sc[MC_CNT_CCM_UNCLICKED_BEFORE_LAST], (unsigned)(lc - __popc(m & ((1u << lc) - 1u))));
             if (model == 3) {
 #pragma unroll
                 for (int r = 0; r < MC_R; r++) {
@@ -135,7 +138,7 @@ __global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32
         }
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < 2 * MC_UBM_SLOTS; k += blockDim.x)
+    for (int k = threadIdx.x; k < MC_PUB_COUNTS; k += blockDim.x)
         if (sc[k]) atomicAdd(&pub_counts[k], (unsigned long long)sc[k]);
 }
 
@@ -302,6 +305,7 @@ int mc_model::build_tiles() {
                 t.qd_begin = lo;
                 t.qd_count = (int)(hi - lo);
                 t.blk_off = 0;
+                t.s_packed = t.s_count;
                 tiles.push_back(t);
             }
             continue;
@@ -317,6 +321,7 @@ int mc_model::build_tiles() {
             open = true;
         }
         cur.s_count += (int)sc;
+        cur.s_packed = cur.s_count;
         cur.qd_count = (int)(hi - cur.qd_begin);
     }
     close();
@@ -357,7 +362,7 @@ int mc_model::build_tiles() {
     grid = std::max(1, std::min(n_tiles, per_sm * n_sm));
     int rc2 = write_fit_desc();
     if (rc2) return rc2;
-    CK(launch_pack_tiles(d_tiles, n_tiles, wqd, d_pidx, stride, d_click, d_tblk, d_status, n_sm, 0));
+    CK(launch_pack_tiles(model, d_tiles, n_tiles, wqd, spt, d_pidx, stride, d_click, d_tblk, d_status, n_sm, 0));
     CK(cudaDeviceSynchronize());
     int status = 0;
     CK(cudaMemcpy(&status, d_status, 4, cudaMemcpyDeviceToHost));
@@ -491,7 +496,7 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
         (rc = dalloc(&d_seg_begin, (size_t)(n_seg + 1), &scratch)) ||
         (rc = dalloc(&d_seg_lo, (size_t)std::max<int64_t>(n_seg, 1), &scratch)) ||
         (rc = dalloc(&d_seg_hi, (size_t)std::max<int64_t>(n_seg, 1), &scratch)) ||
-        (rc = dalloc(&d_flag, 1, &scratch)) || (rc = dalloc(&d_pub_counts, 2 * MC_UBM_SLOTS, &scratch))) {
+        (rc = dalloc(&d_flag, 1, &scratch)) || (rc = dalloc(&d_pub_counts, MC_PUB_COUNTS, &scratch))) {
         free_scratch();
         return rc;
     }
@@ -506,7 +511,7 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     ck(cudaMemcpyAsync(d_seg_lo, init_lo.data(), init_lo.size() * 4, cudaMemcpyHostToDevice, st));
     ck(cudaMemcpyAsync(d_seg_hi, init_hi.data(), init_hi.size() * 4, cudaMemcpyHostToDevice, st));
     ck(cudaMemsetAsync(d_flag, 0, 4, st));
-    ck(cudaMemsetAsync(d_pub_counts, 0, 2 * MC_UBM_SLOTS * 8, st));
+    ck(cudaMemsetAsync(d_pub_counts, 0, MC_PUB_COUNTS * 8, st));
     ck(cudaMemsetAsync(m->d_pidx, 0, (size_t)(m->stride * MC_R) * 4, st));
     ck(cudaMemsetAsync(m->d_cnt, 0, (size_t)qd_alloc * sizeof(uint2), st));
     if (n && e == cudaSuccess) {
@@ -516,7 +521,7 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
         ck(cudaGetLastError());
     }
     int flag = 0;
-    std::vector<unsigned long long> pub_counts(2 * MC_UBM_SLOTS, 0);
+    std::vector<unsigned long long> pub_counts(MC_PUB_COUNTS, 0);
     std::vector<int> lo(init_lo.size()), hi(init_hi.size());
     ck(cudaMemcpyAsync(&flag, d_flag, 4, cudaMemcpyDeviceToHost, st));
     ck(cudaMemcpyAsync(pub_counts.data(), d_pub_counts, pub_counts.size() * 8, cudaMemcpyDeviceToHost, st));
@@ -547,6 +552,17 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     for (int k = 0; k < m->n_pub; k++) {
         double num = 1.0, den = 2.0;
         if (m->model == MC_PBM) { num += (double)pub_counts[(size_t)k]; den += (double)n; }
+        // Ranks before a session's last click contribute exactly (1, 1) to the
+        // DBN gamma and, when unclicked, to the CCM tau_1 (the z = 0 factor of
+        // such a rank is zero); sessions without clicks contribute (10, 10).
+        if (m->model == MC_DBN) {
+            num += (double)pub_counts[MC_CNT_DBN_BEFORE_LAST];
+            den += (double)pub_counts[MC_CNT_DBN_BEFORE_LAST];
+        }
+        if (m->model == MC_CCM && k == 0) {
+            num += (double)pub_counts[MC_CNT_CCM_UNCLICKED_BEFORE_LAST];
+            den += (double)pub_counts[MC_CNT_CCM_UNCLICKED_BEFORE_LAST];
+        }
         if (m->model == MC_UBM) {
             double w = (double)pub_counts[(size_t)k], wc = (double)pub_counts[(size_t)(MC_UBM_SLOTS + k)];
             num += wc;
