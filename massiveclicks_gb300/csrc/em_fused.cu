@@ -413,12 +413,12 @@ __device__ __forceinline__ float clamp_f(float v) { return v < MC_TOP ? v : MC_T
 __device__ __forceinline__ void mstep_qd_f(int model, int mode, uint2 cnt, float v0, float v1, float* atr, float* sat) {
     float occ = (float)cnt.x, clk = (float)cnt.y;
     float den = model == CCM ? 2.0f + occ + clk : 2.0f + occ;
-    *atr = clamp_f(__fdiv_rn(1.0f + clk + v0, den));
+    *atr = clamp_f(__fdividef(1.0f + clk + v0, den));
     if (model == DBN) {
         float un = occ - clk;
         float sn = mode == PARITY ? 1.0f + un + v1 : 1.0f + v1;
         float sd = mode == PARITY ? 2.0f + clk + 2.0f * un : 2.0f + clk;
-        *sat = clamp_f(__fdiv_rn(sn, sd));
+        *sat = clamp_f(__fdividef(sn, sd));
     }
 }
 
@@ -493,7 +493,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
     __shared__ float pub_th[MC_MAX_PUB];
     __shared__ __align__(8) uint64_t full_bar[FUSED_MAX_STAGES], empty_bar[FUSED_MAX_STAGES];
     __shared__ int stage_tile[FUSED_MAX_STAGES];
-    __shared__ int s_last, s_it, s_abort;
+    __shared__ int s_last, s_it, s_abort, s_chunk;
 
     const Layout L = make_layout(spt, window_max);
     float* bins = reinterpret_cast<float*>(smem + L.bins_off);
@@ -591,25 +591,25 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             uint32_t round = (uint32_t)(k / n_stages);
             // Every consumer thread observes the completed phase itself.
             if (!mbar_wait(&full_bar[st], round & 1u, fits[0].status)) s_abort = 1;
+            if (ctid == 0) s_chunk = 0;
             consumer_sync(nc);
             if (*(volatile int*)&s_abort) break;
             const int t = stage_tile[st];
             if (t < 0) break;
             const TileDev tile = tiles[t];
+            const FitDev& f = fits[tile.fit];
             if (tile.fit != cur_fit) {
                 if (cur_fit >= 0) flush_fit(cur_fit, cur_count);
                 cur_fit = tile.fit;
                 cur_count = 0;
+                // Public values are fixed for the whole launch of a fit.
+                int it = *(volatile int*)f.iter;
+                for (int q = ctid; q < f.n_pub; q += nc) pub_th[q] = f.pub_theta[(it & 1) * MC_MAX_PUB + q];
+                consumer_sync(nc);
             }
-            const FitDev& f = fits[tile.fit];
             const int model = model_of<MODEL>(f);
             const int ns = private_stats(model);
             const int n_pub = f.n_pub;
-            {
-                int it = *(volatile int*)f.iter;
-                for (int q = ctid; q < n_pub; q += nc) pub_th[q] = f.pub_theta[(it & 1) * MC_MAX_PUB + q];
-            }
-            consumer_sync(nc);
 
             const bool direct = tile.qd_count > window_max;
             const unsigned char* sb = smem + L.stage_off + (size_t)st * L.stage_bytes;
@@ -629,17 +629,22 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             SmemSink ssink{bins, ns};
             GlobSink gsink{tile.split >= 0 ? f.split_bins + splits[tile.split].bin_offset : nullptr, ns};
 
-            // ---- E-step over the tile's sessions -------------------------------
+            // ---- E-step: warps take 32-session chunks from a shared counter --
             // Staged tiles hold only the sessions that carry variable statistics
             // (pack_tiles_kernel); direct tiles read every session.
             const int n_sess = direct ? tile.s_count : tile.s_packed;
-            const int rounds = (n_sess + nc - 1) / nc;
+            const int n_chunks = (n_sess + 31) >> 5;
+            auto next_chunk = [&]() {
+                int c = 0;
+                if (lane == 0) c = atomicAdd(&s_chunk, 1);
+                return __shfl_sync(FULL_MASK, c, 0);
+            };
             if (model == PBM) {
                 float acc[MC_R];
 #pragma unroll
                 for (int r = 0; r < MC_R; r++) acc[r] = 0.0f;
-                for (int rd = 0; rd < rounds; rd++) {
-                    int sl = rd * nc + ctid;
+                for (int c = next_chunk(); c < n_chunks; c = next_chunk()) {
+                    int sl = (c << 5) + lane;
                     if (sl < n_sess) {
                         if (direct) estep_pbm(gsrc, gsink, sl, pub_th, acc);
                         else estep_pbm(ssrc, ssink, sl, pub_th, acc);
@@ -651,8 +656,8 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
                     if (lane == 0 && v != 0.0f) atomicAdd(pub_tile + 2 * r, v);
                 }
             } else if (model == UBM) {
-                for (int rd = 0; rd < rounds; rd++) {
-                    int sl = rd * nc + ctid;
+                for (int c = next_chunk(); c < n_chunks; c = next_chunk()) {
+                    int sl = (c << 5) + lane;
                     int key[MC_R];
                     float var[MC_R];
                     if (direct) estep_ubm(gsrc, gsink, sl, sl < n_sess, pub_th, key, var);
@@ -662,8 +667,8 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             } else if (model == DBN) {
                 float gn = 0.0f, gd = 0.0f;
                 const float g = pub_th[0];
-                for (int rd = 0; rd < rounds; rd++) {
-                    int sl = rd * nc + ctid;
+                for (int c = next_chunk(); c < n_chunks; c = next_chunk()) {
+                    int sl = (c << 5) + lane;
                     if (sl < n_sess) {
                         if (direct) estep_dbn(gsrc, gsink, sl, g, gn, gd);
                         else estep_dbn(ssrc, ssink, sl, g, gn, gd);
@@ -675,8 +680,8 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             } else {
                 float tt[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
                 const float t1 = pub_th[0], t2 = pub_th[1], t3 = pub_th[2];
-                for (int rd = 0; rd < rounds; rd++) {
-                    int sl = rd * nc + ctid;
+                for (int c = next_chunk(); c < n_chunks; c = next_chunk()) {
+                    int sl = (c << 5) + lane;
                     if (sl < n_sess) {
                         if (direct) estep_ccm(gsrc, gsink, sl, t1, t2, t3, tt);
                         else estep_ccm(ssrc, ssink, sl, t1, t2, t3, tt);

@@ -170,7 +170,7 @@ struct mc_model {
     std::string fused_reason;
     // query segments of the training set: sessions and qd range
     std::vector<int64_t> seg_begin, seg_lo, seg_hi;
-    int spt = 1024, wqd = 2048, block = 384, stages = 3;
+    int spt = 1024, wqd = 1536, block = 192, stages = 2, ctas_per_sm = 1;
     // fused state
     int32_t* d_pidx = nullptr;
     uint16_t* d_click = nullptr;
@@ -346,20 +346,25 @@ int mc_model::build_tiles() {
     if (!splits.empty()) CK(cudaMemcpy(d_splits, splits.data(), splits.size() * sizeof(SplitDev), cudaMemcpyHostToDevice));
     CK(cudaMemset(d_split_bins, 0, (size_t)std::max<int64_t>(bin_off, 1) * sizeof(double)));
     CK(cudaMemset(d_split_count, 0, std::max<size_t>(splits.size(), 1) * sizeof(unsigned)));
-    // Shared memory: bins plus as many copy stages (2..4) as fit.
+    // Shared memory: bins plus a ring of 2..4 copy stages.  Prefer the stage
+    // count that keeps the most CTAs resident per SM, then the deepest ring.
     int optin = 0;
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
     const size_t static_smem = 4096;
-    stages = 0;
-    for (int ns_ = FUSED_MAX_STAGES; ns_ >= 2; ns_--)
-        if (fused_smem_bytes(model, wqd, spt, ns_) + static_smem <= (size_t)optin) { stages = ns_; break; }
-    if (!stages) return set_error(MC_ERR_INVALID, "tile shape does not fit in shared memory (reduce sessions per tile or window)");
-    size_t smem = fused_smem_bytes(model, wqd, spt, stages);
-    CK(fused_set_smem_limits(smem));
-    int per_sm = 0;
-    CK(fused_occupancy(model, block, smem, &per_sm));
-    if (per_sm < 1) return set_error(MC_ERR_INVALID, "configuration does not fit on an SM (window or block too large)");
-    grid = std::max(1, std::min(n_tiles, per_sm * n_sm));
+    int best_score = -1;
+    size_t best_smem = 0;
+    for (int ns_ = 2; ns_ <= FUSED_MAX_STAGES; ns_++) {
+        size_t sm_ = fused_smem_bytes(model, wqd, spt, ns_);
+        if (sm_ + static_smem > (size_t)optin) break;
+        CK(fused_set_smem_limits(sm_));
+        int per_sm = 0;
+        CK(fused_occupancy(model, block, sm_, &per_sm));
+        int score = per_sm * 16 + ns_;
+        if (per_sm >= 1 && score > best_score) { best_score = score; stages = ns_; best_smem = sm_; ctas_per_sm = per_sm; }
+    }
+    if (best_score < 0) return set_error(MC_ERR_INVALID, "tile shape does not fit in shared memory (reduce sessions per tile or window)");
+    CK(fused_set_smem_limits(best_smem));
+    grid = std::max(1, std::min(n_tiles, ctas_per_sm * n_sm));
     int rc2 = write_fit_desc();
     if (rc2) return rc2;
     CK(launch_pack_tiles(model, d_tiles, n_tiles, wqd, spt, d_pidx, stride, d_click, d_tblk, d_status, n_sm, 0));
@@ -843,8 +848,8 @@ extern "C" int mc_model_autotune(mc_model* m, void* stream) {
     CK(cudaMemcpy(th.data(), m->d_pub_theta, th.size() * 4, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(&it0, m->d_iter, 4, cudaMemcpyDeviceToHost));
     struct Cand { int spt, wqd, block; };
-    const Cand cands[] = {{1024, 2048, 384}, {512, 2048, 384}, {2048, 2048, 384}, {1024, 4096, 384},
-                          {1024, 2048, 256}, {2048, 4096, 256}, {512, 1024, 160}};
+    const Cand cands[] = {{1024, 1536, 192}, {512, 1024, 192}, {1024, 1024, 192}, {2048, 1536, 192},
+                          {1024, 2048, 384}, {2048, 2048, 384}, {512, 1536, 192}, {1024, 1536, 384}};
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
