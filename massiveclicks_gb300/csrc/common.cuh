@@ -21,7 +21,8 @@
 
 // Fused kernel: at most this many threads per CTA (one producer warp plus the
 // consumer warps) and this many shared-memory stages in its copy ring.
-#define FUSED_THREADS 384
+#define FUSED_THREADS 256
+#define FUSED_MIN_CTAS 2
 #define FUSED_MAX_STAGES 4
 
 // Param::value() clamp (click_models/param.cu:116-128).

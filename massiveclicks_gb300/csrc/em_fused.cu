@@ -126,6 +126,8 @@ struct SmemSrc {
         m = clk[sl];
         return true;
     }
+    __device__ __forceinline__ bool head(int sl, unsigned& m) const { m = clk[sl]; return true; }
+    __device__ __forceinline__ int rel_at(int r, int sl) const { return rel[r * spad + sl]; }
     __device__ __forceinline__ float a(int rl) const { return atr[woff + rl]; }
     __device__ __forceinline__ float s(int rl) const { return sat[woff + rl]; }
 };
@@ -150,6 +152,14 @@ struct GlobSrc {
         m = __ldg(clk + s_begin + sl);
         if (!ok) atomicOr(status, ST_BAD_INDEX);
         return ok;
+    }
+    // Click mask, after checking that all ten indices fall inside the window.
+    __device__ __forceinline__ bool head(int sl, unsigned& m) const {
+        int rl[MC_R];
+        return load(sl, rl, m);
+    }
+    __device__ __forceinline__ int rel_at(int r, int sl) const {
+        return (int)((int64_t)__ldg(pidx + (int64_t)r * stride + s_begin + sl) - qd_begin);
     }
     __device__ __forceinline__ float a(int rl) const { return atr[qd_begin + rl]; }
     __device__ __forceinline__ float s(int rl) const { return sat[qd_begin + rl]; }
@@ -253,25 +263,20 @@ __device__ __forceinline__ void rescale(float& P, float& E) {
 // ---------------------------------------------------------------------------
 template <class Src, class Sink>
 __device__ __forceinline__ void estep_dbn(const Src& src, const Sink& sink, int sl, float g, float& gnum, float& gden) {
-    int rl[MC_R];
     unsigned m;
-    if (!src.load(sl, rl, m)) return;
-    int l = m ? 31 - __clz(m) : MC_R;
+    if (!src.head(sl, m)) return;
+    const int l = m ? 31 - __clz(m) : MC_R;
     // Ranks before the last click contribute exactly (1, 1) each, a session
     // without clicks (10, 10) and nothing else: constants of the fit, added to
     // the public M-step at upload (model.cu), so they are skipped here.
     if (l == MC_R) return;
-    float a[MC_R], sv[MC_R];
+    // Only a, car and the all-unclicked prefix products stay in registers;
+    // satisfaction values and window indices are re-read from shared memory.
+    float a[MC_R];
 #pragma unroll
-    for (int r = 0; r < MC_R; r++) {
-        a[r] = src.a(rl[r]);
-        sv[r] = src.s(rl[r]);
-    }
-    // Unconditional examination (compute_exm_car) and car, backwards.
-    float eps[MC_R], car[MC_R + 1];
-    eps[0] = 1.0f;
-#pragma unroll
-    for (int r = 0; r < MC_R - 1; r++) eps[r + 1] = eps[r] * (g * (1.0f - a[r]) + g * a[r] * (1.0f - sv[r]));
+    for (int r = 0; r < MC_R; r++) a[r] = src.a(src.rel_at(r, sl));
+    // car_r = a_r + g (1 - a_r) car_{r+1}, car_10 = 0 (compute_exm_car).
+    float car[MC_R + 1];
     car[MC_R] = 0.0f;
 #pragma unroll
     for (int r = MC_R - 1; r >= 0; r--) car[r] = a[r] + g * (1.0f - a[r]) * car[r + 1];
@@ -286,38 +291,39 @@ __device__ __forceinline__ void estep_dbn(const Src& src, const Sink& sink, int 
             Eu *= g * (1.0f - a[j]);
         }
     }
-    // Conditional examination up to rank l (restarting at every click).
-    float P = 1.0f, E = 1.0f;
-#pragma unroll
-    for (int j = 0; j < MC_R; j++) {
-        if (j < l) {
-            if ((m >> j) & 1u) { E = g * (1.0f - sv[j]); P = 1.0f; }
-            else { P = P - a[j] * E; E = E * g * (1.0f - a[j]); rescale(P, E); }
-        }
-    }
+    // One forward pass: unconditional examination eps_r, the conditional
+    // examination (P, E) restarted at every click, and the statistics of the
+    // ranks from the last click on.
+    float eps = 1.0f, P = 1.0f, E = 1.0f;
 #pragma unroll
     for (int r = 0; r < MC_R; r++) {
-        float R = (r < MC_R - 1) ? Pu[MC_R - 1 - r] : 1.0f;
-        if (r == l) {
+        const int rl = src.rel_at(r, sl);
+        const float s_r = src.s(rl);
+        const float R = (r < MC_R - 1) ? Pu[MC_R - 1 - r] : 1.0f;
+        if (r < l) {
+            if ((m >> r) & 1u) { E = g * (1.0f - s_r); P = 1.0f; }
+            else { P = P - a[r] * E; E = E * g * (1.0f - a[r]); rescale(P, E); }
+        } else if (r == l) {
             // Clicked last rank: satisfaction and gamma.
-            float cs = 1.0f - sv[r];
+            float cs = 1.0f - s_r;
             float w = cs * g;
             float B = __fdividef(1.0f, 1.0f - w * (1.0f - R));
             gnum += w * R * B;
             gden += cs * (1.0f - g + g * R) * B;
-            sink.add(rl[r], 1, __fdividef(sv[r], 1.0f - cs * g * car[r + 1]));
+            sink.add(rl, 1, __fdividef(s_r, 1.0f - cs * g * car[r + 1]));
             E = g * cs;
             P = 1.0f;
-        } else if (r > l) {
+        } else {
             // Unclicked rank after the last click.
             float D = __fdividef(1.0f, P - g * E * (1.0f - R));
             gnum += g * R * E * D;
             gden += E * (1.0f - g * (1.0f - R)) * D;
-            sink.add(rl[r], 0, __fdividef(a[r] * (1.0f - eps[r]), 1.0f - eps[r] * car[r]));
+            sink.add(rl, 0, __fdividef(a[r] * (1.0f - eps), 1.0f - eps * car[r]));
             P = P - a[r] * E;
             E = E * g * (1.0f - a[r]);
             rescale(P, E);
         }
+        eps *= g * (1.0f - a[r]) + g * a[r] * (1.0f - s_r);
     }
 }
 
@@ -328,33 +334,14 @@ __device__ __forceinline__ void estep_dbn(const Src& src, const Sink& sink, int 
 template <class Src, class Sink>
 __device__ __forceinline__ void estep_ccm(const Src& src, const Sink& sink, int sl, float t1, float t2, float t3,
                                           float (&t)[6]) {
-    int rl[MC_R];
     unsigned m;
-    if (!src.load(sl, rl, m)) return;
-    int l = m ? 31 - __clz(m) : MC_R;
+    if (!src.head(sl, m)) return;
+    const int l = m ? 31 - __clz(m) : MC_R;
+    if (l == MC_R) return;  // constant contributions only (added at upload)
     float a[MC_R];
 #pragma unroll
-    for (int r = 0; r < MC_R; r++) a[r] = src.a(rl[r]);
-    // Ranks before the last click.
-#pragma unroll
-    for (int r = 0; r < MC_R; r++) {
-        if (r < l) {
-            // An unclicked rank before the last click adds exactly (1, 1) to
-            // tau_1: a constant of the fit, added at upload (model.cu).
-            if ((m >> r) & 1u) {
-                float x = (1.0f - a[r]) * t2, y = a[r] * t3;
-                float u = __fdividef(x, x + y);
-                t[2] += u; t[3] += u;
-                t[4] += 1.0f - u; t[5] += 1.0f - u;
-            }
-        }
-    }
-    if (l == MC_R) return;
-    float eps[MC_R], car[MC_R + 1];
-    eps[0] = 1.0f;
-#pragma unroll
-    for (int r = 0; r < MC_R - 1; r++)
-        eps[r + 1] = eps[r] * ((1.0f - a[r]) * t1 + a[r] * ((1.0f - a[r]) * t2 + a[r] * t3));
+    for (int r = 0; r < MC_R; r++) a[r] = src.a(src.rel_at(r, sl));
+    float car[MC_R + 1];
     car[MC_R] = 0.0f;
 #pragma unroll
     for (int r = MC_R - 1; r >= 0; r--) car[r] = a[r] + (1.0f - a[r]) * t1 * car[r + 1];
@@ -368,36 +355,47 @@ __device__ __forceinline__ void estep_ccm(const Src& src, const Sink& sink, int 
             Eu *= t1 * (1.0f - a[j]);
         }
     }
-    float P = 1.0f, E = 1.0f;
-#pragma unroll
-    for (int j = 0; j < MC_R; j++) {
-        if (j < l) {
-            if ((m >> j) & 1u) { E = t2 * (1.0f - a[j]) + t3 * a[j]; P = 1.0f; }
-            else { P = P - a[j] * E; E = E * t1 * (1.0f - a[j]); rescale(P, E); }
-        }
-    }
+    float eps = 1.0f, P = 1.0f, E = 1.0f;
 #pragma unroll
     for (int r = 0; r < MC_R; r++) {
-        float R = (r < MC_R - 1) ? Pu[MC_R - 1 - r] : 1.0f;
-        if (r == l) {
-            float ia = 1.0f - a[r];
+        const float R = (r < MC_R - 1) ? Pu[MC_R - 1 - r] : 1.0f;
+        const float ia = 1.0f - a[r];
+        if (r < l) {
+            if ((m >> r) & 1u) {
+                // Clicked rank before the last click: only the tau_2 / tau_3
+                // split depends on the parameters.
+                float x = ia * t2, y = a[r] * t3;
+                float u = __fdividef(x, x + y);
+                t[2] += u; t[3] += u;
+                t[4] += 1.0f - u; t[5] += 1.0f - u;
+                E = t2 * ia + t3 * a[r];
+                P = 1.0f;
+            } else {
+                // An unclicked rank before the last click adds exactly (1, 1)
+                // to tau_1: a constant of the fit, added at upload.
+                P = P - a[r] * E;
+                E = E * t1 * ia;
+                rescale(P, E);
+            }
+        } else if (r == l) {
             float k2 = 1.0f - t2 * (1.0f - R), k3 = 1.0f - t3 * (1.0f - R);
             float B = __fdividef(1.0f, ia * k2 + a[r] * k3);
             t[2] += ia * t2 * R * B; t[3] += ia * k2 * B;
             t[4] += a[r] * t3 * R * B; t[5] += a[r] * k3 * B;
             float cont = t2 * ia + t3 * a[r];
-            sink.add(rl[r], 0, __fdividef(a[r], 1.0f - cont * car[r + 1]));
+            sink.add(src.rel_at(r, sl), 0, __fdividef(a[r], 1.0f - cont * car[r + 1]));
             E = cont;
             P = 1.0f;
-        } else if (r > l) {
+        } else {
             float D = __fdividef(1.0f, P - t1 * E * (1.0f - R));
             t[0] += t1 * R * E * D;
             t[1] += E * (1.0f - t1 * (1.0f - R)) * D;
-            sink.add(rl[r], 0, __fdividef((1.0f - eps[r]) * a[r], 1.0f - eps[r] * car[r]));
+            sink.add(src.rel_at(r, sl), 0, __fdividef((1.0f - eps) * a[r], 1.0f - eps * car[r]));
             P = P - a[r] * E;
-            E = E * t1 * (1.0f - a[r]);
+            E = E * t1 * ia;
             rescale(P, E);
         }
+        eps *= ia * t1 + a[r] * (ia * t2 + a[r] * t3);
     }
 }
 
@@ -484,7 +482,7 @@ __host__ __device__ inline Layout make_layout(int spt, int window_max) {
 }
 
 template <int MODEL>
-__global__ void __launch_bounds__(FUSED_THREADS, 1)
+__global__ void __launch_bounds__(FUSED_THREADS, FUSED_MIN_CTAS)
 em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ tiles, int n_tiles,
                 const SplitDev* __restrict__ splits, WorkState* ws, int window_max, int spt, int n_stages) {
     extern __shared__ __align__(128) unsigned char smem[];

@@ -170,7 +170,7 @@ struct mc_model {
     std::string fused_reason;
     // query segments of the training set: sessions and qd range
     std::vector<int64_t> seg_begin, seg_lo, seg_hi;
-    int spt = 1024, wqd = 1536, block = 192, stages = 2, ctas_per_sm = 1;
+    int spt = 1024, wqd = 1536, block = 256, stages = 2, ctas_per_sm = 1;
     // fused state
     int32_t* d_pidx = nullptr;
     uint16_t* d_click = nullptr;
@@ -848,8 +848,8 @@ extern "C" int mc_model_autotune(mc_model* m, void* stream) {
     CK(cudaMemcpy(th.data(), m->d_pub_theta, th.size() * 4, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(&it0, m->d_iter, 4, cudaMemcpyDeviceToHost));
     struct Cand { int spt, wqd, block; };
-    const Cand cands[] = {{1024, 1536, 192}, {512, 1024, 192}, {1024, 1024, 192}, {2048, 1536, 192},
-                          {1024, 2048, 384}, {2048, 2048, 384}, {512, 1536, 192}, {1024, 1536, 384}};
+    const Cand cands[] = {{1024, 1536, 256}, {512, 1024, 256}, {1024, 1024, 256}, {2048, 1536, 256},
+                          {512, 1024, 160}, {1024, 1536, 192}, {512, 768, 160}, {256, 512, 128}};
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
