@@ -86,7 +86,7 @@ def test_clean_mode_matches_f64_oracle(name):
     assert_params_close(cm.get_parameters(), f.values(), what=f"clean {name}")
 
 
-@pytest.mark.parametrize("config", [(7, 16, 64), (32, 64, 128), (100, 5000, 64), (1024, 4096, 384), (4096, 1024, 256)])
+@pytest.mark.parametrize("config", [(7, 16, 64), (32, 64, 128), (100, 5000, 64), (1024, 4096, 256), (4096, 1024, 256)])
 def test_tiling_does_not_change_results(config):
     """Tiny tiles force queries split over many tiles and windows too wide for
     shared memory; results must not depend on the tile shape."""
@@ -216,7 +216,7 @@ def test_configure_rejects_shapes_that_do_not_fit():
     case = load_case("dbn_dbnclicks")
     cm = gpu_fit(case, 2, 0)
     with pytest.raises(api._capi.MCError):
-        cm.configure(4096, 16384, 384)
+        cm.configure(4096, 16384, 256)
     with pytest.raises(api._capi.MCError):
         cm.configure(0, 0, 1024)
 
