@@ -201,6 +201,32 @@ int mc_model_memory(const mc_model* m, int64_t* bytes);
 /* Replaces destroy_parameters (pbm.cu:445-460 etc.). */
 void mc_model_destroy(mc_model* m);
 
+/* ---------------------------------------------------------------------------
+ * Allocation-free evaluation.  No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory at the moment they evaluate:
+ * a serving process whose device memory is already handed to its own pool, a
+ * job under a memory budget that forbids new allocations, a host thread that
+ * must not enter the allocator (and its implicit synchronisation) while other
+ * streams run.  Computes the same sums as mc_model_evaluate from the caller's
+ * own device buffers into the caller's host memory, keeping its intermediate
+ * sums in a fixed file-scope device array (704 KB on every GPU that loads the
+ * library, held until the process exits) instead of an allocation; it calls
+ * no allocating CUDA or library routine.
+ *
+ * Limit: n_sessions <= 16,777,216; a larger call fails with MC_ERR_INVALID.
+ * Inputs (device memory): pidx session-major [n * 10] (-1 = doc unseen in
+ * training), click_mask [n], atr [n_qd], sat [n_qd] (DBN; NULL otherwise),
+ * pub = the model's public values (PBM 10, UBM 55, DBN 1, CCM 3).
+ * Outputs (host memory): *ll_sum and log2_sums[10], as mc_model_evaluate.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture on that device.  All calls share the
+ * array: calls that overlap on the GPU race, so serialise them.  Synchronous
+ * on `stream`. */
+int mc_evaluate_static(int model_type, int64_t n_sessions, const int32_t* pidx, const uint16_t* click_mask,
+                       int64_t n_qd, const float* atr, const float* sat, const float* pub, double* ll_sum,
+                       double* log2_sums, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

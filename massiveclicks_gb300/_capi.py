@@ -58,6 +58,7 @@ _SIGS = {
     "mc_model_evaluate": (C.c_int, [_VP, C.c_int, C.POINTER(_F64), _VP, C.POINTER(_I64), _VP]),
     "mc_model_memory": (C.c_int, [_VP, C.POINTER(_I64)]),
     "mc_model_destroy": (None, [_VP]),
+    "mc_evaluate_static": (C.c_int, [C.c_int, _I64, _VP, _VP, _I64, _VP, _VP, _VP, C.POINTER(_F64), _VP, _VP]),
 }
 
 _lib: C.CDLL | None = None
