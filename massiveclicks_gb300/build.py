@@ -59,7 +59,7 @@ def _digest(paths: list[Path], extra: str) -> str:
 
 
 def _sources_for_lib() -> list[Path]:
-    hdrs = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list((CSRC / "host").glob("*.h")) + [INCLUDE / "mclicks.h"]
+    hdrs = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list((CSRC / "host").glob("*.h")) + sorted(INCLUDE.glob("*.h*"))
     return CU_SOURCES + HOST_SOURCES + hdrs
 
 

@@ -799,7 +799,8 @@ cudaError_t fused_occupancy(int model, int block, size_t smem, int* blocks_per_s
 // Packs the tiles' sessions into the staged layout: per tile, rank-major
 // uint16 window-relative indices [10][spad] followed by the click masks
 // [spad] (padding zeroed), spad = s_packed rounded up to 8.  Sessions are
-// ordered by click pattern (DBN/CCM: last-click rank; PBM/UBM: click mask), a
+// ordered by click pattern (DBN/CCM: last-click rank, then mask; PBM/UBM:
+// click mask), a
 // stable bitonic sort on (key, position), so the lanes of a warp take the
 // same branches.  DBN and CCM sessions without clicks carry no variable
 // statistic (their constant contributions are folded in at upload) and are
@@ -819,7 +820,7 @@ __global__ void pack_tiles_kernel(int model, TileDev* tiles, int n_tiles, int wi
             uint32_t key = 0xFFFFFFFFu;
             if (i < tile.s_count) {
                 unsigned m = click[tile.s_begin + i];
-                uint32_t k16 = drop_clickless ? (m ? (uint32_t)(31 - __clz(m)) : 0xFFFFu) : m;
+                uint32_t k16 = drop_clickless ? (m ? (((uint32_t)(31 - __clz(m)) << 10) | m) : 0xFFFFu) : m;
                 key = (k16 << 16) | (uint32_t)i;
             }
             keys[i] = key;

@@ -156,6 +156,8 @@ __global__ void build_recs_kernel(int64_t n, int64_t stride, const int32_t* plan
     }
 }
 
+constexpr int kGraphChunk = 64;
+
 struct ParamDesc {
     const char* name;
     int kind;  // 0 = public, 1 = attractiveness, 2 = satisfaction
@@ -198,9 +200,9 @@ struct mc_model {
     uint16_t* d_test_click = nullptr;
     double* d_eval = nullptr;
     int64_t test_bytes = 0;
-    // graph of the fused loop
-    cudaGraphExec_t graph = nullptr;
-    int graph_iters = -1;
+    // graphs of the fused loop: a full chunk and a remainder
+    struct GraphSlot { cudaGraphExec_t exec = nullptr; int iters = -1; };
+    GraphSlot graphs[2];
     cudaStream_t own_stream = nullptr;
 
     std::vector<ParamDesc> params() const {
@@ -213,9 +215,11 @@ struct mc_model {
     }
 
     void drop_graph() {
-        if (graph) cudaGraphExecDestroy(graph);
-        graph = nullptr;
-        graph_iters = -1;
+        for (GraphSlot& g : graphs) {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+            g.iters = -1;
+        }
     }
 
     void free_tiles() {
@@ -658,20 +662,30 @@ extern "C" int mc_model_em(mc_model* m, int32_t iters, int impl, void* stream) {
     if (iters == 0 || m->n == 0) return MC_OK;
     if (impl == MC_IMPL_FUSED) {
         if (!m->fused_ok) return set_error(MC_ERR_INVALID, "model_em: fused path unavailable: " + m->fused_reason);
-        if (!m->graph || m->graph_iters != iters) {
-            m->drop_graph();
-            cudaGraph_t g = nullptr;
-            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            int rc = launch_fused_loop(m, iters, st);
-            cudaError_t e = cudaStreamEndCapture(st, &g);
-            if (rc) { if (g) cudaGraphDestroy(g); return rc; }
-            if (e != cudaSuccess) return cuda_fail("cudaStreamEndCapture", e);
-            e = cudaGraphInstantiate(&m->graph, g, 0);
-            cudaGraphDestroy(g);
-            if (e != cudaSuccess) { m->graph = nullptr; return cuda_fail("cudaGraphInstantiate", e); }
-            m->graph_iters = iters;
+        // The loop is captured as graphs of at most kGraphChunk iterations
+        // (one full chunk, one remainder), each replayed as often as needed.
+        const int full = iters / kGraphChunk, rem = iters % kGraphChunk;
+        for (int pass = 0; pass < 2; pass++) {
+            int len = pass == 0 ? kGraphChunk : rem;
+            int reps = pass == 0 ? full : (rem ? 1 : 0);
+            if (!reps) continue;
+            auto& slot = m->graphs[pass];
+            if (!slot.exec || slot.iters != len) {
+                if (slot.exec) cudaGraphExecDestroy(slot.exec);
+                slot.exec = nullptr;
+                cudaGraph_t g = nullptr;
+                CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                int rc = launch_fused_loop(m, len, st);
+                cudaError_t e = cudaStreamEndCapture(st, &g);
+                if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+                if (e != cudaSuccess) return cuda_fail("cudaStreamEndCapture", e);
+                e = cudaGraphInstantiate(&slot.exec, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) { slot.exec = nullptr; return cuda_fail("cudaGraphInstantiate", e); }
+                slot.iters = len;
+            }
+            for (int k = 0; k < reps; k++) CK(cudaGraphLaunch(slot.exec, st));
         }
-        CK(cudaGraphLaunch(m->graph, st));
     } else {
         int rc = m->ensure_plain(st);
         if (rc) return rc;

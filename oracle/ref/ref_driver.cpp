@@ -18,8 +18,9 @@
 //       parameter (numerator, denominator) after selected iterations, then the
 //       reference's LogLikelihood / Perplexity on the test set
 //       (evaluation.cpp:25-66) and the final reduction (parallel_em.cu:697-723).
-//   em_parallel DATASET MAX_SESSIONS TEST_SHARE MODEL ITERS THREADS
-//       ingest, then the unmodified em_parallel() itself (prints its log lines).
+//   em_parallel DATASET MAX_SESSIONS TEST_SHARE MODEL ITERS THREADS [OUT_PREFIX]
+//       ingest, then the unmodified em_parallel() itself (prints its log lines
+//       and, with OUT_PREFIX, writes its parameter CSVs).
 
 #include <cstdio>
 #include <cstdlib>
@@ -199,9 +200,10 @@ int main(int argc, char** argv) {
         for (int i = 0; i < 10; i++) fprintf(f, "log2sum_%d %a\nppl_%d %a\n", i, ppl.task_rank_perplexities[i], i, ppl_rank[i]);
         fprintf(f, "seconds_per_iteration %.9f\n", total / (iters > 0 ? iters : 1));
         fclose(f);
-    } else if (cmd == "em_parallel" && argc == 8) {
+    } else if (cmd == "em_parallel" && (argc == 8 || argc == 9)) {
         Setup s;
         make_setup(s, argv[2], atoi(argv[3]), (float)atof(argv[4]), atoi(argv[5]), atoi(argv[6]), atoi(argv[7]));
+        if (argc == 9) s.config.output_path = argv[8];  // parameter CSVs (communicator.cpp:423-516)
         em_parallel(s.config, s.partitions);
     } else {
         fprintf(stderr, "bad arguments for %s\n", cmd.c_str());

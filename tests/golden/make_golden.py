@@ -133,9 +133,13 @@ def run_case(driver: Path, name: str, log_text: str, max_sessions: int, models, 
             data[f"m{model}_llh"] = np.float64(ev["llh"])
             data[f"m{model}_ppl"] = np.float64(ev["ppl"])
             data[f"m{model}_log2_sums"] = np.array([ev[f"log2sum_{r}"] for r in range(10)], np.float64)
-            # The driver's loop must agree with the reference's own em_parallel.
+            # The driver's loop must agree with the reference's own em_parallel,
+            # which also writes its parameter CSVs (kept as text for the CLI test).
+            prefix = out / "csv"
             res = subprocess.run([str(driver), "em_parallel", str(log), str(max_sessions), "0.2", str(model),
-                                  str(iters), "1"], check=True, capture_output=True, text=True)
+                                  str(iters), "1", str(prefix)], check=True, capture_output=True, text=True)
+            for csv in sorted(out.glob("csv_*.csv")):
+                data[f"m{model}_csv_{csv.stem[4:]}"] = np.frombuffer(csv.read_bytes(), np.uint8)
             llh_line = [x for x in res.stdout.splitlines() if x.startswith("Total Log likelihood is:")][0]
             em_llh = float(llh_line.split(":")[1])
             assert abs(em_llh - ev["llh"]) <= 1e-5 * abs(ev["llh"]), (em_llh, ev["llh"])
