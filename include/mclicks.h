@@ -202,6 +202,28 @@ int mc_model_memory(const mc_model* m, int64_t* bytes);
 void mc_model_destroy(mc_model* m);
 
 /* ---------------------------------------------------------------------------
+ * Batched fits: several independent fits (any mix of model types, e.g. one per
+ * query partition) advanced together, one persistent launch per iteration over
+ * the union of their tiles.  The reference runs one model per process
+ * (parallel_em/parallel_em.cu:364-372); this replaces many such runs.
+ * ------------------------------------------------------------------------- */
+typedef struct mc_batch mc_batch;
+
+/* The models must be uploaded and on one device; every model is given the
+ * first model's tile shape.  Models keep their own parameters and may still be
+ * used alone; they must not be re-uploaded or reconfigured while the batch
+ * exists. */
+int mc_batch_create(int n_models, mc_model* const* models, mc_batch** out);
+
+/* n_iterations fused iterations of every model, captured as CUDA graphs and
+ * replayed.  NULL stream = internal stream, synchronous. */
+int mc_batch_em(mc_batch* b, int32_t n_iterations, void* stream);
+
+int mc_batch_info(const mc_batch* b, int32_t* n_models, int32_t* n_tiles, int32_t* mixed_models);
+
+void mc_batch_destroy(mc_batch* b);
+
+/* ---------------------------------------------------------------------------
  * Allocation-free evaluation.  No counterpart in the reference.
  *
  * For callers that cannot allocate device memory at the moment they evaluate:

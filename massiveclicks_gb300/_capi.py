@@ -58,6 +58,10 @@ _SIGS = {
     "mc_model_evaluate": (C.c_int, [_VP, C.c_int, C.POINTER(_F64), _VP, C.POINTER(_I64), _VP]),
     "mc_model_memory": (C.c_int, [_VP, C.POINTER(_I64)]),
     "mc_model_destroy": (None, [_VP]),
+    "mc_batch_create": (C.c_int, [C.c_int, _VP, C.POINTER(_VP)]),
+    "mc_batch_em": (C.c_int, [_VP, _I32, _VP]),
+    "mc_batch_info": (C.c_int, [_VP, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32)]),
+    "mc_batch_destroy": (None, [_VP]),
     "mc_evaluate_static": (C.c_int, [C.c_int, _I64, _VP, _VP, _I64, _VP, _VP, _VP, C.POINTER(_F64), _VP, _VP]),
 }
 

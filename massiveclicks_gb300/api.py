@@ -292,6 +292,35 @@ class UBMModel(ClickModel):
     model_type = UBM
 
 
+class Batch:
+    """Several fits advanced together, one persistent launch per iteration."""
+
+    def __init__(self, models: list):
+        self.models = list(models)
+        arr = (C.c_void_p * len(self.models))(*[m._h.value for m in self.models])
+        self._h = C.c_void_p()
+        check(_capi.load().mc_batch_create(len(self.models), C.cast(arr, C.c_void_p), C.byref(self._h)))
+
+    def em(self, iterations: int, stream=None) -> None:
+        check(_capi.load().mc_batch_em(self._h, int(iterations), _stream(stream)))
+
+    def info(self) -> tuple[int, int, bool]:
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        check(_capi.load().mc_batch_info(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, bool(c.value)
+
+    def close(self) -> None:
+        if self._h:
+            _capi.load().mc_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def em_parallel(model_type: int, dataset: Dataset, iterations: int = 50, mode: int = MODE_PARITY,
                 impl: int = IMPL_FUSED, device: int = 0) -> tuple[ClickModel, Evaluation]:
     """em_parallel (parallel_em/parallel_em.cu:349-746) for one GPU: upload,

@@ -201,7 +201,7 @@ struct mc_model {
     double* d_eval = nullptr;
     int64_t test_bytes = 0;
     // graphs of the fused loop: a full chunk and a remainder
-    struct GraphSlot { cudaGraphExec_t exec = nullptr; int iters = -1; };
+    struct GraphSlot { cudaGraphExec_t exec = nullptr; int iters = -1; };  // also used by mc_batch
     GraphSlot graphs[2];
     cudaStream_t own_stream = nullptr;
 
@@ -264,6 +264,7 @@ struct mc_model {
 
     int64_t qd_alloc() const { return ((std::max<int64_t>(n_qd, 1) + 3) & ~(int64_t)3) + 4; }
     int build_tiles();
+    FitDev make_desc() const;
     int write_fit_desc();
     int ensure_plain(cudaStream_t st);
 };
@@ -367,7 +368,10 @@ int mc_model::build_tiles() {
         if (per_sm >= 1 && score > best_score) { best_score = score; stages = ns_; best_smem = sm_; ctas_per_sm = per_sm; }
     }
     if (best_score < 0) return set_error(MC_ERR_INVALID, "tile shape does not fit in shared memory (reduce sessions per tile or window)");
-    CK(fused_set_smem_limits(best_smem));
+    // The attribute is per kernel, shared by every model and batch: keep it at
+    // the device maximum so no configuration can shrink it under another one.
+    (void)best_smem;
+    CK(fused_set_smem_limits((size_t)optin - static_smem));
     grid = std::max(1, std::min(n_tiles, ctas_per_sm * n_sm));
     int rc2 = write_fit_desc();
     if (rc2) return rc2;
@@ -379,7 +383,7 @@ int mc_model::build_tiles() {
     return MC_OK;
 }
 
-int mc_model::write_fit_desc() {
+FitDev mc_model::make_desc() const {
     FitDev f{};
     f.model = model;
     f.mode = mode;
@@ -402,6 +406,11 @@ int mc_model::write_fit_desc() {
     f.tiles_done = d_tiles_done;
     f.iter = d_iter;
     f.status = d_status;
+    return f;
+}
+
+int mc_model::write_fit_desc() {
+    FitDev f = make_desc();
     CK(cudaMemcpy(d_fit, &f, sizeof(f), cudaMemcpyHostToDevice));
     return MC_OK;
 }
@@ -920,4 +929,173 @@ extern "C" int mc_model_init_parameters(mc_model* m, void* stream) {
     CK(cudaMemsetAsync(m->d_iter, 0, 4, st));
     CK(cudaStreamSynchronize(st));
     return MC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batches: several fits in one persistent launch per iteration
+// ---------------------------------------------------------------------------
+struct mc_batch {
+    std::vector<mc_model*> models;
+    int device = 0, n_sm = 0, kernel_model = -1;
+    int spt = 0, wqd = 0, block = 0, stages = 2, grid = 1, n_tiles = 0;
+    FitDev* d_fits = nullptr;
+    TileDev* d_tiles = nullptr;
+    SplitDev* d_splits = nullptr;
+    WorkState* d_ws = nullptr;
+    mc_model::GraphSlot graphs[2];
+    cudaStream_t own_stream = nullptr;
+    int64_t bytes = 0;
+
+    void release() {
+        for (auto& g : graphs) { if (g.exec) cudaGraphExecDestroy(g.exec); g.exec = nullptr; g.iters = -1; }
+        dfree(d_fits); dfree(d_tiles); dfree(d_splits); dfree(d_ws);
+        if (own_stream) cudaStreamDestroy(own_stream);
+        own_stream = nullptr;
+    }
+};
+
+static int batch_launch_loop(mc_batch* b, int iters, cudaStream_t st) {
+    for (int i = 0; i < iters; i++)
+        CK(launch_em_fused(b->kernel_model, b->d_fits, b->d_tiles, b->n_tiles, b->d_splits, b->d_ws, b->wqd, b->spt,
+                           b->stages, b->grid, b->block, st));
+    return MC_OK;
+}
+
+extern "C" int mc_batch_create(int n_models, mc_model* const* models, mc_batch** out) {
+    if (!out || !models || n_models < 1) return set_error(MC_ERR_INVALID, "batch_create: need at least one model");
+    *out = nullptr;
+    for (int i = 0; i < n_models; i++) {
+        mc_model* m = models[i];
+        if (!m || !m->uploaded) return set_error(MC_ERR_STATE, "batch_create: every model must have uploaded sessions");
+        if (!m->fused_ok) return set_error(MC_ERR_INVALID, "batch_create: model " + std::to_string(i) + ": " + m->fused_reason);
+        if (m->device != models[0]->device) return set_error(MC_ERR_INVALID, "batch_create: models on different devices");
+    }
+    mc_model* m0 = models[0];
+    CK(cudaSetDevice(m0->device));
+    // One tile shape for the whole launch: the first model's.
+    for (int i = 1; i < n_models; i++) {
+        mc_model* m = models[i];
+        if (m->spt != m0->spt || m->wqd != m0->wqd || m->block != m0->block) {
+            int rc = mc_model_configure(m, m0->spt, m0->wqd, m0->block);
+            if (rc) return rc;
+        }
+    }
+    mc_batch* b = new (std::nothrow) mc_batch();
+    if (!b) return set_error(MC_ERR_NOMEM, "batch_create: out of host memory");
+    b->models.assign(models, models + n_models);
+    b->device = m0->device;
+    b->n_sm = m0->n_sm;
+    b->spt = m0->spt;
+    b->wqd = m0->wqd;
+    b->block = m0->block;
+    b->kernel_model = m0->model;
+    std::vector<FitDev> fits;
+    std::vector<TileDev> tiles;
+    std::vector<SplitDev> splits;
+    for (int i = 0; i < n_models; i++) {
+        mc_model* m = models[i];
+        if (m->model != b->kernel_model) b->kernel_model = -1;
+        fits.push_back(m->make_desc());
+        std::vector<TileDev> t((size_t)m->n_tiles);
+        std::vector<SplitDev> sp((size_t)m->n_splits);
+        cudaError_t e = cudaSuccess;
+        if (!t.empty()) e = cudaMemcpy(t.data(), m->d_tiles, t.size() * sizeof(TileDev), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && !sp.empty()) e = cudaMemcpy(sp.data(), m->d_splits, sp.size() * sizeof(SplitDev), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) { delete b; return cuda_fail("batch_create", e); }
+        int split_off = (int)splits.size();
+        for (TileDev& x : t) {
+            x.fit = i;
+            if (x.split >= 0) x.split += split_off;
+            tiles.push_back(x);
+        }
+        splits.insert(splits.end(), sp.begin(), sp.end());
+    }
+    b->n_tiles = (int)tiles.size();
+    int rc;
+    if ((rc = dalloc(&b->d_fits, fits.size(), &b->bytes)) || (rc = dalloc(&b->d_tiles, tiles.size(), &b->bytes)) ||
+        (rc = dalloc(&b->d_splits, splits.size(), &b->bytes)) || (rc = dalloc(&b->d_ws, 1, &b->bytes))) {
+        b->release();
+        delete b;
+        return rc;
+    }
+    cudaError_t e = cudaMemcpy(b->d_fits, fits.data(), fits.size() * sizeof(FitDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !tiles.empty()) e = cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !splits.empty()) e = cudaMemcpy(b->d_splits, splits.data(), splits.size() * sizeof(SplitDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(b->d_ws, 0, sizeof(WorkState));
+    if (e != cudaSuccess) { b->release(); delete b; return cuda_fail("batch_create", e); }
+    // Shared memory and occupancy of the common launch.
+    int optin = 0;
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
+    int best = -1;
+    size_t best_smem = 0;
+    for (int ns_ = 2; ns_ <= FUSED_MAX_STAGES && e == cudaSuccess; ns_++) {
+        size_t sm_ = fused_smem_bytes(b->kernel_model, b->wqd, b->spt, ns_);
+        if (sm_ + 4096 > (size_t)optin) break;
+        if ((e = fused_set_smem_limits(sm_)) != cudaSuccess) break;
+        int per_sm = 0;
+        if ((e = fused_occupancy(b->kernel_model, b->block, sm_, &per_sm)) != cudaSuccess) break;
+        int score = per_sm * 16 + ns_;
+        if (per_sm >= 1 && score > best) { best = score; b->stages = ns_; best_smem = sm_; b->grid = per_sm; }
+    }
+    if (e == cudaSuccess && best >= 0) e = fused_set_smem_limits((size_t)optin - 4096);
+    (void)best_smem;
+    if (e != cudaSuccess || best < 0) {
+        b->release();
+        delete b;
+        return e != cudaSuccess ? cuda_fail("batch_create", e) : set_error(MC_ERR_INVALID, "batch_create: tile shape does not fit");
+    }
+    b->grid = std::max(1, std::min(b->n_tiles, b->grid * b->n_sm));
+    *out = b;
+    return MC_OK;
+}
+
+extern "C" int mc_batch_em(mc_batch* b, int32_t iters, void* stream) {
+    if (!b) return set_error(MC_ERR_INVALID, "batch_em: null batch");
+    if (iters < 0) return set_error(MC_ERR_INVALID, "batch_em: negative iteration count");
+    CK(cudaSetDevice(b->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!st) {
+        if (!b->own_stream) CK(cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking));
+        st = b->own_stream;
+    }
+    if (iters == 0 || b->n_tiles == 0) return MC_OK;
+    const int full = iters / kGraphChunk, rem = iters % kGraphChunk;
+    for (int pass = 0; pass < 2; pass++) {
+        int len = pass == 0 ? kGraphChunk : rem;
+        int reps = pass == 0 ? full : (rem ? 1 : 0);
+        if (!reps) continue;
+        auto& slot = b->graphs[pass];
+        if (!slot.exec || slot.iters != len) {
+            if (slot.exec) cudaGraphExecDestroy(slot.exec);
+            slot.exec = nullptr;
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            int rc = batch_launch_loop(b, len, st);
+            cudaError_t e = cudaStreamEndCapture(st, &g);
+            if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+            if (e != cudaSuccess) return cuda_fail("cudaStreamEndCapture", e);
+            e = cudaGraphInstantiate(&slot.exec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { slot.exec = nullptr; return cuda_fail("cudaGraphInstantiate", e); }
+            slot.iters = len;
+        }
+        for (int k = 0; k < reps; k++) CK(cudaGraphLaunch(slot.exec, st));
+    }
+    if (!stream) CK(cudaStreamSynchronize(st));
+    return MC_OK;
+}
+
+extern "C" int mc_batch_info(const mc_batch* b, int32_t* n_models, int32_t* n_tiles, int32_t* mixed_models) {
+    if (!b) return set_error(MC_ERR_INVALID, "batch_info: null batch");
+    if (n_models) *n_models = (int32_t)b->models.size();
+    if (n_tiles) *n_tiles = b->n_tiles;
+    if (mixed_models) *mixed_models = b->kernel_model < 0;
+    return MC_OK;
+}
+
+extern "C" void mc_batch_destroy(mc_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->device);
+    b->release();
+    delete b;
 }
