@@ -43,8 +43,8 @@ DATA = ("synthetic: 20M sessions, 1M queries Zipf(1.0), 50-doc pools, top-10 sho
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--sessions", type=int, default=20_000_000)
     ap.add_argument("--queries", type=int, default=1_000_000)
@@ -54,6 +54,9 @@ def parse_args():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--workload", choices=["dbn20m", "batched"], default="dbn20m",
+                    help="dbn20m: the headline DBN fit; batched: 256 mixed fits in one launch")
+    ap.add_argument("--batch-fits", type=int, default=256)
     return ap.parse_args()
 
 
@@ -402,9 +405,81 @@ def run_ours(args, rank: int, world: int, local: int):
     dist.close()
 
 
+def run_batched(args, rank: int, world: int, local: int):
+    """256 independent fits (PBM/UBM/DBN in turn) on disjoint query partitions
+    of log-uniform size 1k..500k sessions (about 30M in total), generated like
+    the 40k-session PBM workload (1k queries Zipf 1.1 per partition, 20-doc
+    pools, PBM clicks).  One step = one EM iteration of every fit.  Compared:
+    one persistent launch for all fits (mc_batch_em) against each fit's own
+    fused launch and each fit's plain two-kernel EM, run one after another."""
+    import torch
+    from massiveclicks_gb300 import api
+    from massiveclicks_gb300._capi import IMPL_FUSED, IMPL_PLAIN
+
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(4242 + rank)
+    sizes = np.exp(rng.uniform(np.log(1000), np.log(500000), args.batch_fits)).astype(np.int64)
+    types = [0, 3, 2]
+    models, n_train = [], 0
+    t0 = time.perf_counter()
+    for i, n in enumerate(sizes):
+        cfg = api.synth_config(0, n_sessions=int(n), n_queries=1000, seed=9000 + 7919 * i + rank)
+        q, d, m = api.synth_sessions(cfg)
+        ds = api.Dataset.from_sessions(q, d, m, 0.2)
+        cm = api.ClickModel.create(types[i % 3])
+        cm.upload(ds.train, ds.n_qd)
+        models.append(cm)
+        n_train += len(ds.train)
+    prep_s = time.perf_counter() - t0
+    stream = torch.cuda.Stream()
+    batch = api.Batch(models)
+    n_fits, n_tiles, _ = batch.info()
+
+    def timed(fn, steps):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    batch.em(args.warmup, stream)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms_batch = timed(lambda k: batch.em(k, stream), args.steps)
+    clk = clocks.stop()
+    for cm in models:
+        cm.em(1, IMPL_FUSED, stream)
+    ms_sep = timed(lambda k: [cm.em(k, IMPL_FUSED, stream) for cm in models], max(1, args.steps // 4))
+    plain_steps = 2
+    for cm in models:
+        cm.em(1, IMPL_PLAIN, stream)
+    ms_plain = timed(lambda k: [cm.em(k, IMPL_PLAIN, stream) for cm in models], plain_steps)
+    value = n_train / (ms_batch / 1000.0)
+    if rank == 0:
+        line = {
+            "metric": "EM session-iterations/s, 256 batched fits (mixed PBM/UBM/DBN)", "value": value, "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_batch,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: per fit 1k queries Zipf(1.1), 20-doc pools, PBM clicks; sizes log-uniform 1k..500k",
+            "config": {"workload": f"{n_fits} fits, {int(sizes.sum())} sessions ({n_train} training), one launch per "
+                                   "iteration for all fits", "tiles": n_tiles, "prep_s": round(prep_s, 2)},
+            "separate_fused": {"value": n_train / (ms_sep / 1000.0), "ms_per_step": ms_sep},
+            "separate_plain": {"value": n_train / (ms_plain / 1000.0), "ms_per_step": ms_plain,
+                               "batched_speedup": ms_plain / ms_batch},
+            "gpu_launches": args.steps, "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
+    if args.impl == "ours" and args.workload == "batched":
+        run_batched(args, rank, world, local)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
     else:
