@@ -211,7 +211,8 @@ public:
 // the reference's result lines.
 void em_parallel(const ProcessingConfig& config, LocalPartitions& device_partitions);
 
-// The parameter CSVs of communicator.cpp:423-516 for one worker.
+// The parameter CSVs of communicator.cpp:423-516 for one worker (private
+// parameter files carry no header line, as the reference's do).
 void output_parameters(const std::string& file_path, const Partition& partition, ClickModel_Hst* cm);
 
 }  // namespace mclicks

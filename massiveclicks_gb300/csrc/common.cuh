@@ -80,7 +80,9 @@ struct SplitDev {
     int64_t qd_begin;
     int qd_count;
     int n_tiles;
-    int64_t bin_offset; // into split_bins, in doubles
+    int64_t bin_offset; // into the fit's split_bins, in doubles
+    int local;          // index of this split query's counter in the fit's split_count
+    int pad_;
 };
 
 struct WorkState {

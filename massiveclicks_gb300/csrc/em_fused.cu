@@ -715,7 +715,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
                 __threadfence();
                 consumer_sync(nc);
                 if (ctid == 0) {
-                    unsigned old = atomicAdd(f.split_count + tile.split, 1u);
+                    unsigned old = atomicAdd(f.split_count + sp.local, 1u);
                     s_last = (old + 1 == (unsigned)sp.n_tiles);
                 }
                 consumer_sync(nc);
@@ -730,7 +730,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
                         gb[(int64_t)i * ns] = 0.0;
                         if (ns > 1) gb[(int64_t)i * ns + 1] = 0.0;
                     }
-                    if (ctid == 0) f.split_count[tile.split] = 0;
+                    if (ctid == 0) f.split_count[sp.local] = 0;
                 }
             }
 

@@ -249,8 +249,8 @@ void Perplexity::evaluate(ClickModel_Hst* cm, TestSet& testing_queries) {
 
 // ---------------------------------------------------------------------------
 // Parameter CSVs (communicator.cpp:423-516, one worker): public parameters
-// as "rank, value"; private ones as "query, document, value", one line per
-// training session and rank, 0.5 for an index of -1.
+// as "rank, value" under a header line; private ones as "query, document,
+// value", one line per training session and rank, 0.5 for an index of -1.
 // ---------------------------------------------------------------------------
 void output_parameters(const std::string& file_path, const Partition& partition, ClickModel_Hst* cm) {
     std::pair<std::vector<std::string>, std::vector<std::string>> headers;
@@ -266,8 +266,10 @@ void output_parameters(const std::string& file_path, const Partition& partition,
     for (size_t k = 0; k < headers.second.size(); k++) {
         std::string path = file_path + "_" + headers.second[k] + ".csv";
         std::cout << "  Writing parameter " << headers.second[k] << " to " << path << std::endl;
+        // The reference writes this header, then writes the data from offset
+        // 0 of the same file (MPI_File_write_at_all), which overwrites it: its
+        // files hold the data lines only, and so do these.
         std::ofstream f(path);
-        f << "query, document, " << headers.second[k] << std::endl;
         const std::vector<Param>& v = *params.second[k];
         std::string data;
         for (const SERP_Hst& s : std::get<0>(partition)) {

@@ -297,6 +297,8 @@ int mc_model::build_tiles() {
             sp.qd_count = (int)(hi - lo);
             sp.n_tiles = nt;
             sp.bin_offset = bin_off;
+            sp.local = (int)splits.size();
+            sp.pad_ = 0;
             bin_off += (hi - lo) * ns;
             int sid = (int)splits.size();
             splits.push_back(sp);

@@ -16,8 +16,12 @@ pytestmark = pytest.mark.gpu
 
 
 def _csv_rows(text: str):
+    """(header or None, rows).  The reference's private-parameter files have no
+    header: its data write at offset 0 overwrites the header line."""
     lines = text.strip().splitlines()
-    return lines[0], [tuple(x.strip() for x in l.split(",")) for l in lines[1:]]
+    head = lines[0] if not lines[0][:1].isdigit() and not lines[0].startswith("-") else None
+    body = lines[1:] if head is not None else lines
+    return head, [tuple(x.strip() for x in l.split(",")) for l in body]
 
 
 @pytest.mark.parametrize("name,model", [("dbn_dbnclicks", 2), ("pbm_pbmclicks", 0), ("ccm_ccmclicks", 1),
