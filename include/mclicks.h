@@ -224,6 +224,27 @@ int mc_batch_info(const mc_batch* b, int32_t* n_models, int32_t* n_tiles, int32_
 void mc_batch_destroy(mc_batch* b);
 
 /* ---------------------------------------------------------------------------
+ * DBN log-likelihood as a function of logit parameters, and its gradient: a
+ * forward/backward pair shaped like an autograd function.  The likelihood is
+ * the reference's conditional DBN click probability (click_models/dbn.cu:611-639)
+ * summed over training sessions [s_begin, s_begin + s_count) of the model's
+ * uploaded set, with attractiveness a = sigmoid(alpha[qd]), satisfaction
+ * s = sigmoid(beta[qd]) and continuation g = sigmoid(gamma[0]).  alpha and beta
+ * ([n_qd]) and gamma ([1]) are device arrays.  fp64 = 1 evaluates in double
+ * precision (for verification), 0 in single; sums are FP64 either way.
+ * ------------------------------------------------------------------------- */
+int mc_dbn_loglik_forward(mc_model* m, int64_t s_begin, int64_t s_count, const float* alpha, const float* beta,
+                          const float* gamma, int fp64, double* loglik, void* stream);
+
+/* Writes grad_output * d(log-likelihood)/d(alpha, beta, gamma) to the device
+ * arrays d_alpha, d_beta ([n_qd]) and d_gamma ([1]), overwriting them; the
+ * forward messages are recomputed, not stored.  *loglik (optional) receives
+ * the log-likelihood. */
+int mc_dbn_loglik_backward(mc_model* m, int64_t s_begin, int64_t s_count, const float* alpha, const float* beta,
+                           const float* gamma, int fp64, double grad_output, float* d_alpha, float* d_beta,
+                           float* d_gamma, double* loglik, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Allocation-free evaluation.  No counterpart in the reference.
  *
  * For callers that cannot allocate device memory at the moment they evaluate:

@@ -62,6 +62,9 @@ _SIGS = {
     "mc_batch_em": (C.c_int, [_VP, _I32, _VP]),
     "mc_batch_info": (C.c_int, [_VP, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32)]),
     "mc_batch_destroy": (None, [_VP]),
+    "mc_dbn_loglik_forward": (C.c_int, [_VP, _I64, _I64, _VP, _VP, _VP, C.c_int, C.POINTER(_F64), _VP]),
+    "mc_dbn_loglik_backward": (C.c_int, [_VP, _I64, _I64, _VP, _VP, _VP, C.c_int, _F64, _VP, _VP, _VP,
+                                         C.POINTER(_F64), _VP]),
     "mc_evaluate_static": (C.c_int, [C.c_int, _I64, _VP, _VP, _I64, _VP, _VP, _VP, C.POINTER(_F64), _VP, _VP]),
 }
 

@@ -60,6 +60,24 @@ struct EvalArgs {
 
 cudaError_t launch_eval(const EvalArgs& A, int n_sm, cudaStream_t st);
 
+// ---- DBN log-likelihood adjoint (adjoint.cu) ---------------------------------
+struct AdjointArgs {
+    int64_t begin, count, stride;
+    const int32_t* pidx;     // [10][stride]
+    const uint16_t* click;
+    const float* alpha;      // logits [n_qd]
+    const float* beta;       // logits [n_qd]
+    const float* gamma;      // logit [1]
+    double scale;            // gradient scale (the caller's grad_output)
+    double* g_alpha;         // FP64 gradient accumulators
+    double* g_beta;
+    double* g_gamma;
+    double* ll_out;          // log-likelihood sum
+};
+
+cudaError_t launch_adjoint(const AdjointArgs& A, bool grad, bool fp64, int n_sm, cudaStream_t st);
+cudaError_t launch_grad_to_float(const double* src, float* dst, int64_t n, int n_sm, cudaStream_t st);
+
 }  // namespace mcd
 
 #endif  // MCLICKS_KERNELS_H

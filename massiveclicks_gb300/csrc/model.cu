@@ -194,6 +194,9 @@ struct mc_model {
     float2 *d_atr2 = nullptr, *d_sat2 = nullptr, *d_pub2 = nullptr, *d_tmp_atr = nullptr, *d_tmp_sat = nullptr,
            *d_tmp_pub = nullptr;
     int64_t plain_bytes = 0;
+    // FP64 gradient accumulators of the adjoint (allocated on first use):
+    // [alpha: qd_alloc][beta: qd_alloc][gamma][log-likelihood]
+    double* d_grad = nullptr;
     // evaluation set
     int64_t n_test = 0, test_stride = 0;
     int32_t* d_test_pidx = nullptr;
@@ -244,7 +247,7 @@ struct mc_model {
         free_plain();
         dfree(d_pidx); dfree(d_click); dfree(d_cnt); dfree(d_atr); dfree(d_sat); dfree(d_pub_theta);
         dfree(d_pub_bins); dfree(d_pub_const); dfree(d_tiles_done); dfree(d_iter); dfree(d_status);
-        dfree(d_fit); dfree(d_ws);
+        dfree(d_fit); dfree(d_ws); dfree(d_grad);
         bytes = test_bytes;
         uploaded = false;
     }
@@ -1100,4 +1103,79 @@ extern "C" void mc_batch_destroy(mc_batch* b) {
     cudaSetDevice(b->device);
     b->release();
     delete b;
+}
+
+// ---------------------------------------------------------------------------
+// DBN log-likelihood and its adjoint (adjoint.cu)
+// ---------------------------------------------------------------------------
+static int adjoint_common(mc_model* m, int64_t s_begin, int64_t s_count, const float* alpha, const float* beta,
+                          const float* gamma, const char* who) {
+    if (!m) return set_error(MC_ERR_INVALID, std::string(who) + ": null model");
+    if (!m->uploaded) return set_error(MC_ERR_STATE, std::string(who) + ": no training sessions uploaded");
+    if (s_begin < 0 || s_count < 0 || s_begin + s_count > m->n)
+        return set_error(MC_ERR_INVALID, std::string(who) + ": session range outside the training set");
+    if (s_count > 0 && (!alpha || !beta || !gamma)) return set_error(MC_ERR_INVALID, std::string(who) + ": null parameter");
+    CK(cudaSetDevice(m->device));
+    if (!m->d_grad) {
+        int64_t before = m->bytes;
+        int rc = dalloc(&m->d_grad, (size_t)(2 * m->qd_alloc() + 2), &m->bytes);
+        if (rc) return rc;
+        (void)before;
+    }
+    return MC_OK;
+}
+
+static AdjointArgs adjoint_args(mc_model* m, int64_t s_begin, int64_t s_count, const float* alpha, const float* beta,
+                                const float* gamma, double scale) {
+    AdjointArgs A;
+    A.begin = s_begin;
+    A.count = s_count;
+    A.stride = m->stride;
+    A.pidx = m->d_pidx;
+    A.click = m->d_click;
+    A.alpha = alpha;
+    A.beta = beta;
+    A.gamma = gamma;
+    A.scale = scale;
+    A.g_alpha = m->d_grad;
+    A.g_beta = m->d_grad + m->qd_alloc();
+    A.g_gamma = m->d_grad + 2 * m->qd_alloc();
+    A.ll_out = m->d_grad + 2 * m->qd_alloc() + 1;
+    return A;
+}
+
+extern "C" int mc_dbn_loglik_forward(mc_model* m, int64_t s_begin, int64_t s_count, const float* alpha,
+                                     const float* beta, const float* gamma, int fp64, double* loglik, void* stream) {
+    int rc = adjoint_common(m, s_begin, s_count, alpha, beta, gamma, "dbn_loglik_forward");
+    if (rc) return rc;
+    if (!loglik) return set_error(MC_ERR_INVALID, "dbn_loglik_forward: null output");
+    cudaStream_t st = m->pick(stream);
+    AdjointArgs A = adjoint_args(m, s_begin, s_count, alpha, beta, gamma, 0.0);
+    CK(cudaMemsetAsync(A.ll_out, 0, 8, st));
+    CK(launch_adjoint(A, false, fp64 != 0, m->n_sm, st));
+    CK(cudaMemcpyAsync(loglik, A.ll_out, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return MC_OK;
+}
+
+extern "C" int mc_dbn_loglik_backward(mc_model* m, int64_t s_begin, int64_t s_count, const float* alpha,
+                                      const float* beta, const float* gamma, int fp64, double grad_output,
+                                      float* d_alpha, float* d_beta, float* d_gamma, double* loglik, void* stream) {
+    int rc = adjoint_common(m, s_begin, s_count, alpha, beta, gamma, "dbn_loglik_backward");
+    if (rc) return rc;
+    if (!d_alpha || !d_beta || !d_gamma) return set_error(MC_ERR_INVALID, "dbn_loglik_backward: null gradient output");
+    cudaStream_t st = m->pick(stream);
+    AdjointArgs A = adjoint_args(m, s_begin, s_count, alpha, beta, gamma, grad_output);
+    CK(cudaMemsetAsync(m->d_grad, 0, (size_t)(2 * m->qd_alloc() + 2) * 8, st));
+    CK(launch_adjoint(A, true, fp64 != 0, m->n_sm, st));
+    CK(launch_grad_to_float(A.g_alpha, d_alpha, m->n_qd, m->n_sm, st));
+    CK(launch_grad_to_float(A.g_beta, d_beta, m->n_qd, m->n_sm, st));
+    CK(launch_grad_to_float(A.g_gamma, d_gamma, 1, m->n_sm, st));
+    if (loglik) {
+        CK(cudaMemcpyAsync(loglik, A.ll_out, 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    } else if (!stream) {
+        CK(cudaStreamSynchronize(st));
+    }
+    return MC_OK;
 }

@@ -45,6 +45,9 @@ def load() -> C.CDLL:
     lib.orc_fit_set_values.argtypes = [vp, vp]
     lib.orc_fit_eval.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, vp]
     lib.orc_fit_free.argtypes = [vp]
+    lib.orc_dbn_loglik.restype = C.c_double
+    lib.orc_dbn_loglik.argtypes = [C.c_int64, vp, vp, vp, vp, C.c_double]
+    lib.orc_dbn_fisher.argtypes = [C.c_int64, vp, vp, vp, vp, C.c_double, vp, vp, vp]
     _lib = lib
     return lib
 
@@ -134,3 +137,25 @@ class OracleFit:
                 self.h = None
         except Exception:
             pass
+
+
+def dbn_loglik(pidx, click_mask, alpha, beta, gamma: float) -> float:
+    """FP64 DBN log-likelihood (conditional model of the reference) of sessions."""
+    p = np.ascontiguousarray(pidx, np.int32).reshape(-1)
+    m = np.ascontiguousarray(click_mask, np.uint16)
+    a = np.ascontiguousarray(alpha, np.float64)
+    b = np.ascontiguousarray(beta, np.float64)
+    return load().orc_dbn_loglik(m.shape[0], _p(p), _p(m), _p(a), _p(b), float(gamma))
+
+
+def dbn_fisher(pidx, click_mask, alpha, beta, gamma: float):
+    """Expected complete-data scores under the exact DBN posterior (Fisher identity)."""
+    p = np.ascontiguousarray(pidx, np.int32).reshape(-1)
+    m = np.ascontiguousarray(click_mask, np.uint16)
+    a = np.ascontiguousarray(alpha, np.float64)
+    b = np.ascontiguousarray(beta, np.float64)
+    sa = np.zeros_like(a)
+    sb = np.zeros_like(b)
+    sg = C.c_double(0.0)
+    load().orc_dbn_fisher(m.shape[0], _p(p), _p(m), _p(a), _p(b), float(gamma), _p(sa), _p(sb), C.byref(sg))
+    return sa, sb, sg.value

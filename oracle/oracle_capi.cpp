@@ -90,7 +90,96 @@ void eval(const Fit<T>& f, int64_t n_test, const int32_t* pidx, const uint16_t* 
 
 }  // namespace
 
+// DBN log-likelihood of the reference's conditional model (dbn.cu:611-639)
+// in FP64, with a = sigmoid(alpha), s = sigmoid(beta), g = sigmoid(gamma).
+double dbn_loglik(int64_t n, const int32_t* pidx, const uint16_t* click, const double* alpha, const double* beta,
+                  double gamma) {
+    auto sg = [](double x) { return 1.0 / (1.0 + std::exp(-x)); };
+    double g = sg(gamma), ll = 0.0;
+    for (int64_t i = 0; i < n; i++) {
+        double ex = 1.0;
+        for (int r = 0; r < R; r++) {
+            int32_t p = pidx[i * R + r];
+            double a = sg(alpha[p]), s = sg(beta[p]), pr;
+            if ((click[i] >> r) & 1) { pr = a * ex; ex = g * (1.0 - s); }
+            else { pr = 1.0 - a * ex; ex = ex * g * (1.0 - a) / pr; }
+            ll += std::log(pr);
+        }
+    }
+    return ll;
+}
+
+// Fisher-identity scores of the same likelihood: the expected complete-data
+// score under the exact DBN posterior (a textbook forward-backward over the
+// examination chain, not the reference's E-step), with respect to the logits.
+//   alpha: clicked occurrence (1 - a); unclicked -a P(E_r = 1 | clicks)
+//   beta:  clicked before the last click -s; last click P(S = 1 | clicks) - s
+//   gamma: per transition r -> r+1 (r <= 8) from an examined state that may
+//          continue: P(E_{r+1} = 1, eligible) - g P(eligible)
+void dbn_fisher(int64_t n, const int32_t* pidx, const uint16_t* click, const double* alpha, const double* beta,
+                double gamma, double* s_alpha, double* s_beta, double* s_gamma) {
+    auto sg = [](double x) { return 1.0 / (1.0 + std::exp(-x)); };
+    double g = sg(gamma);
+    *s_gamma = 0.0;
+    for (int64_t i = 0; i < n; i++) {
+        unsigned m = click[i];
+        double a[R], s[R];
+        int p[R];
+        for (int r = 0; r < R; r++) { p[r] = pidx[i * R + r]; a[r] = sg(alpha[p[r]]); s[r] = sg(beta[p[r]]); }
+        int l = -1;
+        for (int r = R - 1; r >= 0; r--) if ((m >> r) & 1u) { l = r; break; }
+        // backward: b[r] = P(no clicks at r..9 | E_r = 1), for ranks after l
+        double b[R + 1];
+        b[R] = 1.0;
+        for (int r = R - 1; r > l; r--) b[r] = (1.0 - a[r]) * (g * b[r + 1] + (1.0 - g));
+        // forward after l: f[r] = P(E_r = 1, no clicks in (l, r) | history)
+        double f[R + 1] = {0};
+        int first = l + 1;
+        double start = l >= 0 ? (1.0 - s[l]) * g : 1.0;  // P(E_{l+1} = 1 | click at l) or E_0 = 1
+        if (first < R) f[first] = start;
+        for (int r = first; r < R - 1; r++) f[r + 1] = f[r] * (1.0 - a[r]) * g;
+        // Z = P(no clicks after l | history)
+        double Z = l >= 0 ? (s[l] + (1.0 - s[l]) * ((1.0 - g) + g * (l + 1 < R ? b[l + 1] : 1.0))) : b[0];
+        if (l >= 0 && l + 1 >= R) Z = 1.0;
+        auto pe = [&](int r) {  // P(E_r = 1 | clicks)
+            if (r <= l) return 1.0;
+            if (r >= R) return 0.0;
+            return f[r] * b[r] / Z;
+        };
+        for (int r = 0; r < R; r++) {
+            if ((m >> r) & 1u) s_alpha[p[r]] += 1.0 - a[r];
+            else s_alpha[p[r]] += -a[r] * pe(r);
+            if ((m >> r) & 1u) {
+                if (r < l) s_beta[p[r]] += -s[r];
+                else if (l + 1 < R) s_beta[p[r]] += s[r] / Z - s[r];
+                else s_beta[p[r]] += 0.0;  // last rank: satisfaction does not affect the likelihood
+            }
+        }
+        for (int r = 0; r < R - 1; r++) {
+            if (r < l) {
+                *s_gamma += 1.0 - g;
+            } else if (r == l) {
+                double p_cont = f[l + 1] * b[l + 1] / Z;       // P(S_l = 0, E_{l+1} = 1 | clicks)
+                double p_elig = 1.0 - s[l] / Z;                 // P(S_l = 0 | clicks)
+                *s_gamma += p_cont - g * p_elig;
+            } else {
+                *s_gamma += pe(r + 1) - g * pe(r);
+            }
+        }
+    }
+}
+
 extern "C" {
+
+double orc_dbn_loglik(int64_t n, const int32_t* pidx, const uint16_t* click, const double* alpha, const double* beta,
+                      double gamma) {
+    return dbn_loglik(n, pidx, click, alpha, beta, gamma);
+}
+
+void orc_dbn_fisher(int64_t n, const int32_t* pidx, const uint16_t* click, const double* alpha, const double* beta,
+                    double gamma, double* s_alpha, double* s_beta, double* s_gamma) {
+    dbn_fisher(n, pidx, click, alpha, beta, gamma, s_alpha, s_beta, s_gamma);
+}
 
 void* orc_parse(const char* path, int max_sessions, float test_share) {
     std::vector<Session> raw;

@@ -1,0 +1,135 @@
+"""The DBN log-likelihood adjoint (mc_dbn_loglik_forward/backward) against
+FP64 central finite differences of the oracle's likelihood (step 1e-4) and,
+through the Fisher identity, against the expected complete-data scores of the
+exact DBN posterior computed by the oracle."""
+import numpy as np
+import pytest
+
+from conftest import load_case
+from massiveclicks_gb300 import api, gradient
+from oracle import bindings
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _setup(name="dbn_dbnclicks", seed=0):
+    case = load_case(name)
+    n_qd = int(case["n_qd"])
+    cm = api.DBNModel()
+    cm.upload(api.SessionSet(case["train_query"], case["train_docs"], case["train_pidx"], case["train_click"]), n_qd)
+    rng = np.random.default_rng(seed)
+    al = rng.normal(-1.0, 1.0, n_qd).astype(np.float32)
+    be = rng.normal(-1.0, 1.0, n_qd).astype(np.float32)
+    ga = np.array([1.5], np.float32)
+    return case, cm, al, be, ga
+
+
+def _grads(cm, al, be, ga, fp64):
+    dev = torch.device("cuda", 0)
+    a = torch.tensor(al, device=dev, requires_grad=True)
+    b = torch.tensor(be, device=dev, requires_grad=True)
+    g = torch.tensor(ga, device=dev, requires_grad=True)
+    ll = gradient.dbn_loglik(a, b, g, cm, fp64=fp64)
+    ll.backward()
+    return float(ll), a.grad.cpu().numpy().astype(np.float64), b.grad.cpu().numpy().astype(np.float64), \
+        float(g.grad.cpu().numpy()[0])
+
+
+def test_forward_matches_oracle():
+    case, cm, al, be, ga = _setup()
+    ref = bindings.dbn_loglik(case["train_pidx"], case["train_click"], al.astype(np.float64), be.astype(np.float64),
+                              float(ga[0]))
+    ll64, *_ = _grads(cm, al, be, ga, True)
+    ll32, *_ = _grads(cm, al, be, ga, False)
+    assert ll64 == pytest.approx(ref, rel=1e-12)
+    assert ll32 == pytest.approx(ref, rel=1e-6)
+
+
+def test_gradient_matches_central_differences():
+    """1,000 random parameters, FP64 central differences with step 1e-4."""
+    case, cm, al, be, ga = _setup(seed=1)
+    _, ga_, gb_, gg_ = _grads(cm, al, be, ga, True)
+    p, m = case["train_pidx"], case["train_click"]
+    A, B = al.astype(np.float64), be.astype(np.float64)
+    G = float(ga[0])
+    h = 1e-4
+    rng = np.random.default_rng(2)
+    n_qd = A.shape[0]
+    picks = [("a", int(i)) for i in rng.choice(n_qd, 600, replace=False)] + \
+            [("b", int(i)) for i in rng.choice(n_qd, 399, replace=False)] + [("g", 0)]
+    worst = 0.0
+    for kind, i in picks:
+        if kind == "a":
+            x1, x2 = A.copy(), A.copy()
+            x1[i] += h; x2[i] -= h
+            fd = (bindings.dbn_loglik(p, m, x1, B, G) - bindings.dbn_loglik(p, m, x2, B, G)) / (2 * h)
+            got = ga_[i]
+        elif kind == "b":
+            x1, x2 = B.copy(), B.copy()
+            x1[i] += h; x2[i] -= h
+            fd = (bindings.dbn_loglik(p, m, A, x1, G) - bindings.dbn_loglik(p, m, A, x2, G)) / (2 * h)
+            got = gb_[i]
+        else:
+            fd = (bindings.dbn_loglik(p, m, A, B, G + h) - bindings.dbn_loglik(p, m, A, B, G - h)) / (2 * h)
+            got = gg_
+        # relative 1e-6; parameters whose gradient is ~0 (never affect the
+        # likelihood) compare absolutely
+        err = abs(got - fd) / max(abs(fd), 1e-3)
+        worst = max(worst, err)
+    assert worst <= 1e-6, worst
+
+
+def test_gradient_equals_fisher_scores():
+    case, cm, al, be, ga = _setup(seed=3)
+    _, ga_, gb_, gg_ = _grads(cm, al, be, ga, True)
+    sa, sb, sg = bindings.dbn_fisher(case["train_pidx"], case["train_click"], al.astype(np.float64),
+                                     be.astype(np.float64), float(ga[0]))
+    np.testing.assert_allclose(ga_, sa, rtol=1e-7, atol=1e-7)
+    np.testing.assert_allclose(gb_, sb, rtol=1e-7, atol=1e-7)
+    assert gg_ == pytest.approx(sg, rel=1e-7)
+
+
+def test_fp32_gradient_close_to_fp64():
+    case, cm, al, be, ga = _setup(seed=4)
+    _, a64, b64, g64 = _grads(cm, al, be, ga, True)
+    _, a32, b32, g32 = _grads(cm, al, be, ga, False)
+    np.testing.assert_allclose(a32, a64, rtol=1e-4, atol=1e-5)
+    np.testing.assert_allclose(b32, b64, rtol=1e-4, atol=1e-5)
+    assert g32 == pytest.approx(g64, rel=1e-4)
+
+
+def test_ranges_add_up():
+    case, cm, al, be, ga = _setup(seed=5)
+    dev = torch.device("cuda", 0)
+    a = torch.tensor(al, device=dev)
+    b = torch.tensor(be, device=dev)
+    g = torch.tensor(ga, device=dev)
+    n = cm.n_train
+    whole = float(gradient.dbn_loglik(a, b, g, cm, 0, n, fp64=True))
+    parts = float(gradient.dbn_loglik(a, b, g, cm, 0, 1000, fp64=True)) + \
+        float(gradient.dbn_loglik(a, b, g, cm, 1000, n - 1000, fp64=True))
+    assert parts == pytest.approx(whole, rel=1e-12)
+
+
+def test_adam_improves_likelihood():
+    case = load_case("dbn_ccmclicks")
+    n_qd = int(case["n_qd"])
+    train = gradient.shuffled_sessions(api.SessionSet(case["train_query"], case["train_docs"], case["train_pidx"],
+                                                      case["train_click"]))
+    cm = api.DBNModel()
+    cm.upload(train, n_qd)
+    dev = torch.device("cuda", 0)
+    z = torch.zeros(n_qd, device=dev)
+    before = float(gradient.dbn_loglik(z, z, torch.zeros(1, device=dev), cm))
+    a, b, g = gradient.train_adam(cm, n_qd, steps=60, batch=1024, lr=0.05)
+    after = float(gradient.dbn_loglik(a.detach(), b.detach(), g.detach(), cm))
+    assert after > before + 0.05 * abs(before)
+
+
+def test_bad_range_rejected():
+    _, cm, al, be, ga = _setup()
+    dev = torch.device("cuda", 0)
+    a = torch.tensor(al, device=dev)
+    with pytest.raises(api._capi.MCError):
+        gradient.dbn_loglik(a, a, torch.tensor(ga, device=dev), cm, cm.n_train, 5)
