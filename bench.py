@@ -54,6 +54,7 @@ def parse_args():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
     ap.add_argument("--workload", choices=["dbn20m", "batched", "adjoint"], default="dbn20m",
                     help="dbn20m: the headline DBN fit; batched: 256 mixed fits in one launch; "
                          "adjoint: EM against the gradient trainer")
@@ -375,7 +376,7 @@ def run_ours(args, rank: int, world: int, local: int):
                        "iterations + mc_model_get_param of every array + destroy"}
 
     cpu = None
-    if rank == 0:
+    if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         n = cpu_sample(ds, args.cpu_sample)
         times = time_cpu_oracle(ds, n, 2, 1, threads)
@@ -479,7 +480,7 @@ def run_adjoint(args, rank: int, world: int, local: int):
     """DBN on 5M sessions (DBN-generated, 250k queries, 30-doc pools): EM
     (fused, 50 iterations from the prior) against Adam on the logits (lr 0.05,
     batches of 262,144 sessions, the adjoint kernel for gradients), compared on
-    wall time to reach EM's final test log-likelihood, and the adjoint's own
+    wall time to reach EM's best test log-likelihood, and the adjoint's own
     throughput."""
     import torch
     from massiveclicks_gb300 import api, gradient
@@ -501,7 +502,7 @@ def run_adjoint(args, rank: int, world: int, local: int):
         torch.cuda.synchronize()
         t_em += time.perf_counter() - t0
         em_curve.append((t_em, em.evaluate(1).llh))
-    target = em_curve[-1][1]
+    target = max(ll for _, ll in em_curve)  # EM's best test LL within 50 iterations
     t_em_target = next(t for t, ll in em_curve if ll >= target - 1e-4 * abs(target))
 
     trainer_model = api.DBNModel(device=local)
@@ -541,12 +542,13 @@ def run_adjoint(args, rank: int, world: int, local: int):
     ms_grad = e0.elapsed_time(e1) / k
     if rank == 0:
         line = {
-            "metric": "seconds to reach EM's 50-iteration test LL (DBN, 5M sessions): EM vs Adam",
+            "metric": "seconds for Adam to reach EM's best 50-iteration test LL (DBN, 5M sessions)",
             "value": reach[1] if reach else None, "unit": "s", "higher_is_better": False, "n_gpus": world,
             "dtype": "f32", "data": "synthetic: 5M sessions, 250k queries Zipf(1.0), 30-doc pools, DBN clicks",
             "config": {"workload": "DBN EM (fused, from the prior) vs Adam lr 0.05, batch 262,144 sessions",
                        "train_sessions": n_train, "n_qd": n_qd},
-            "em": {"target_test_llh": target, "seconds_to_target": t_em_target, "seconds_50_iterations": t_em},
+            "em": {"target_test_llh": target, "seconds_to_target": t_em_target, "seconds_50_iterations": t_em,
+                   "final_test_llh": em_curve[-1][1]},
             "adam": {"reached": reach is not None, "steps": reach[0] if reach else None,
                      "seconds": reach[1] if reach else None, "final_test_llh": curve[-1][2] if curve else None,
                      "best_test_llh": max(ll for _, _, ll in curve) if curve else None},

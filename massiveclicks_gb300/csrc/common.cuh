@@ -51,6 +51,8 @@ struct FitDev {
     const int32_t* pidx;   // [10][stride], rank-major planes
     const uint16_t* click; // [n] bit masks
     const uint2* cnt;      // [n_qd] {occurrences, clicked occurrences}
+    const uint32_t* cnt16; // [n_qd] occurrences | clicked << 16, each saturated at
+                           // 65535 (exact for qd of whole-query tiles: <= 10 * 4096)
     const unsigned char* tblk;  // packed tile blocks (uint16 window-relative indices + clicks)
     float* atr;            // [n_qd] current values
     float* sat;            // [n_qd] current values (DBN)

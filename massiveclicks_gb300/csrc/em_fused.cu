@@ -3,22 +3,26 @@
 //
 // Work: a queue of session tiles (host-built, see model.cu).  Each tile is a
 // run of whole queries (or a chunk of one large query) whose qd indices form
-// one contiguous window.  One CTA per SM:
+// one contiguous window.  Persistent CTAs (two per SM):
 //   * a producer warp takes the next tile from the global queue and issues
 //     bulk async copies (cp.async.bulk, completion on an mbarrier) of the tile's
 //     packed sessions (uint16 window-relative indices, rank-major, and click
-//     masks) and of the window's parameter values and click counts into a ring
-//     of shared-memory stages;
-//   * consumer warps wait on the stage's mbarrier, run the E-step with one
-//     thread per session entirely from shared memory, add each private
-//     statistic into a shared-memory bin per qd (shared atomics) and each
-//     public statistic into registers, then
+//     masks) and of the window's parameter values into a ring of
+//     shared-memory stages;
+//   * consumer warps wait on the stage's mbarrier; then, as one pool of
+//     warp-sized items taken from a shared counter, they run the E-step of
+//     that tile (one thread per session, entirely from shared memory, each
+//     private statistic added into a shared-memory bin per qd, each public one
+//     into registers) and the M-step of the tile before it, whose bins are in
+//     the other of two bin buffers:
 //       - owned tile (whole queries): M-step for the window straight from the
-//         bins and counts, written in place to global memory (no other tile
-//         reads those parameters);
-//       - split tile (part of a large query): bins are folded into FP64 global
-//         bins, and the last tile of that query runs its M-step;
-//     and release the stage to the producer (second mbarrier).
+//         bins and the click counts, written in place to global memory (no
+//         other tile reads those parameters);
+//       - split tile (part of a large query): one warp folds the bins into the
+//         query's FP64 global bins, and the warp that completes the query's
+//         last tile runs its M-step;
+//     one barrier ends the item pool, and the stage goes back to the producer
+//     (second mbarrier).
 //   * public statistics: warp shuffles -> shared FP32 partial per tile -> FP64
 //     per-CTA accumulator -> one FP64 global atomic per bin per CTA; the CTA
 //     that completes the fit's last tile runs the public M-step into the other
@@ -82,11 +86,33 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait: about 2^26 polls with back-off (several seconds) before giving up.
+// try_wait that may suspend the thread until the phase completes or about
+// `ns` nanoseconds pass (the suspend-time hint), instead of polling.
+__device__ __forceinline__ bool mbar_try_wait_for(uint64_t* bar, uint32_t parity, uint32_t ns) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(ns)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait: gives up after 4 s of wall-clock time (and, should the timer
+// not advance, after 2^24 rounds of at least 256 ns each).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status) {
-    for (uint32_t i = 0; i < (1u << 26); i++) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if (i > 32) __nanosleep(64);
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (uint32_t i = 0; i < (1u << 24); i++) {
+        if (mbar_try_wait_for(bar, parity, 200000u)) return true;
+        if (global_ns() - t0 > 4000000000ull) break;
+        __nanosleep(256);
     }
     atomicOr(status, ST_TIMEOUT);
     return false;
@@ -165,10 +191,12 @@ struct GlobSrc {
     __device__ __forceinline__ float s(int rl) const { return sat[qd_begin + rl]; }
 };
 
+// Statistic k of window entry rl at bins[k * stride + rl]: each statistic is
+// a contiguous array, so the lanes' random entries spread over all 32 banks.
 struct SmemSink {
     float* bins;
-    int ns;
-    __device__ __forceinline__ void add(int rl, int k, float v) const { atomicAdd(bins + rl * ns + k, v); }
+    int stride;
+    __device__ __forceinline__ void add(int rl, int k, float v) const { atomicAdd(bins + k * stride + rl, v); }
 };
 struct GlobSink {
     double* bins;
@@ -291,9 +319,11 @@ __device__ __forceinline__ void estep_dbn(const Src& src, const Sink& sink, int 
             Eu *= g * (1.0f - a[j]);
         }
     }
-    // One forward pass: unconditional examination eps_r, the conditional
-    // examination (P, E) restarted at every click, and the statistics of the
-    // ranks from the last click on.
+    // One forward pass: the unconditional examination eps_r at every rank;
+    // from the last click on, the conditional examination (P, E), which the
+    // click at l restarts (so nothing before l feeds it), and the statistics.
+    // Ranks before l depend on the session only through l, so warps of
+    // sessions sorted by l take one branch per rank.
     float eps = 1.0f, P = 1.0f, E = 1.0f;
 #pragma unroll
     for (int r = 0; r < MC_R; r++) {
@@ -301,8 +331,6 @@ __device__ __forceinline__ void estep_dbn(const Src& src, const Sink& sink, int 
         const float s_r = src.s(rl);
         const float R = (r < MC_R - 1) ? Pu[MC_R - 1 - r] : 1.0f;
         if (r < l) {
-            if ((m >> r) & 1u) { E = g * (1.0f - s_r); P = 1.0f; }
-            else { P = P - a[r] * E; E = E * g * (1.0f - a[r]); rescale(P, E); }
         } else if (r == l) {
             // Clicked last rank: satisfaction and gamma.
             float cs = 1.0f - s_r;
@@ -361,21 +389,15 @@ __device__ __forceinline__ void estep_ccm(const Src& src, const Sink& sink, int 
         const float R = (r < MC_R - 1) ? Pu[MC_R - 1 - r] : 1.0f;
         const float ia = 1.0f - a[r];
         if (r < l) {
+            // Before the last click (P, E) is not needed: the click at l
+            // restarts it.  A clicked rank: only the tau_2 / tau_3 split
+            // depends on the parameters.  An unclicked rank adds exactly
+            // (1, 1) to tau_1: a constant of the fit, added at upload.
             if ((m >> r) & 1u) {
-                // Clicked rank before the last click: only the tau_2 / tau_3
-                // split depends on the parameters.
                 float x = ia * t2, y = a[r] * t3;
                 float u = __fdividef(x, x + y);
                 t[2] += u; t[3] += u;
                 t[4] += 1.0f - u; t[5] += 1.0f - u;
-                E = t2 * ia + t3 * a[r];
-                P = 1.0f;
-            } else {
-                // An unclicked rank before the last click adds exactly (1, 1)
-                // to tau_1: a constant of the fit, added at upload.
-                P = P - a[r] * E;
-                E = E * t1 * ia;
-                rescale(P, E);
             }
         } else if (r == l) {
             float k2 = 1.0f - t2 * (1.0f - R), k3 = 1.0f - t3 * (1.0f - R);
@@ -455,31 +477,40 @@ __device__ void finalize_public(const FitDev& f, int ctid, int nc, int* s_it) {
     }
 }
 
-template <int MODEL>
-__device__ __forceinline__ int model_of(const FitDev& f) { return MODEL >= 0 ? MODEL : f.model; }
-
 // Shared-memory layout of one CTA (dynamic part), all 16-byte aligned:
-//   bins     float [window_max * 2]
+//   bins     float [2 buffers][nb statistics][window_max]; the k-th tile a
+//            CTA takes accumulates into buffer k & 1 (nb = 2 when satisfaction
+//            is a private statistic, else 1)
+//   counts   uint32 [2 slots][window_max + 8]: the window's 16-bit click-count
+//            pairs of the k-th tile in slot k & 1, read by its M-step
 //   stage s  { uint16 rel[10][spt_pad], uint16 clk[spt_pad],
-//              float atr[window_max + 8], float sat[window_max + 8],
-//              uint2 cnt[window_max + 8] }           for s < n_stages
+//              float atr[window_max + 8], float sat[window_max + 8] (DBN) }
+//            for s < n_stages
 struct Layout {
-    uint32_t bins_off, stage_off, stage_bytes, sess_bytes, atr_off, sat_off, cnt_off;
+    uint32_t bins_stride, bins_buf, cnt_off, cnt_slot, stage_off, stage_bytes, sess_bytes, atr_off, sat_off;
 };
 
-__host__ __device__ inline Layout make_layout(int spt, int window_max) {
+__host__ __device__ inline int layout_stats(int model) { return (model == DBN || model < 0) ? 2 : 1; }
+
+__host__ __device__ inline Layout make_layout(int model, int spt, int window_max) {
     Layout L;
-    uint32_t spad = (uint32_t)((spt + 7) & ~7);
-    uint32_t w = (uint32_t)window_max + 8;
-    L.bins_off = 0;
-    L.stage_off = ((uint32_t)window_max * 2 * 4 + 15) & ~15u;
-    L.sess_bytes = 11u * spad * 2;
-    L.atr_off = (L.sess_bytes + 15) & ~15u;
-    L.sat_off = L.atr_off + w * 4;
-    L.cnt_off = L.sat_off + w * 4;
-    L.stage_bytes = (L.cnt_off + w * 8 + 15) & ~15u;
+    const uint32_t spad = (uint32_t)((spt + 7) & ~7);
+    const uint32_t w = (uint32_t)window_max + 8;
+    const uint32_t nb = (uint32_t)layout_stats(model);
+    L.bins_stride = (uint32_t)window_max;
+    L.bins_buf = nb * (uint32_t)window_max;
+    L.cnt_off = (2u * L.bins_buf * 4u + 15u) & ~15u;
+    L.cnt_slot = w;
+    L.stage_off = L.cnt_off + ((2u * w * 4u + 15u) & ~15u);
+    L.sess_bytes = 11u * spad * 2u;
+    L.atr_off = (L.sess_bytes + 15u) & ~15u;
+    L.sat_off = L.atr_off + w * 4u;
+    L.stage_bytes = (L.sat_off + (nb > 1 ? w * 4u : 0u) + 15u) & ~15u;
     return L;
 }
+
+template <int MODEL>
+__device__ __forceinline__ int model_of(const FitDev& f) { return MODEL >= 0 ? MODEL : f.model; }
 
 template <int MODEL>
 __global__ void __launch_bounds__(FUSED_THREADS, FUSED_MIN_CTAS)
@@ -487,28 +518,35 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
                 const SplitDev* __restrict__ splits, WorkState* ws, int window_max, int spt, int n_stages) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ double pub_acc[MC_MAX_PUB];
-    __shared__ float pub_tile[MC_MAX_PUB];
+    __shared__ float pub_tile[2][MC_MAX_PUB];
     __shared__ float pub_th[MC_MAX_PUB];
-    __shared__ __align__(8) uint64_t full_bar[FUSED_MAX_STAGES], empty_bar[FUSED_MAX_STAGES];
+    __shared__ __align__(8) uint64_t full_bar[FUSED_MAX_STAGES], empty_bar[FUSED_MAX_STAGES], cnt_bar[2];
     __shared__ int stage_tile[FUSED_MAX_STAGES];
+    __shared__ TileDev stage_desc[FUSED_MAX_STAGES];   // the staged tile's descriptor (producer)
+    __shared__ TileDev s_desc[2];                      // consumers: the k-th tile's descriptor in slot k & 1
+    __shared__ __align__(16) FitDev s_fit[2];          // consumers: current fit and the one before
     __shared__ int s_last, s_it, s_abort, s_chunk;
 
-    const Layout L = make_layout(spt, window_max);
-    float* bins = reinterpret_cast<float*>(smem + L.bins_off);
+    const Layout L = make_layout(MODEL, spt, window_max);
+    float* bins = reinterpret_cast<float*>(smem);
+    uint32_t* cnt_slots = reinterpret_cast<uint32_t*>(smem + L.cnt_off);
     const int tid = threadIdx.x;
     const int nc = blockDim.x - 32;            // consumer threads; the last warp produces
     const bool producer = tid >= nc;
-    const int* status_any = fits[0].status;
+    int* const status = fits[0].status;
+    static_assert(sizeof(FitDev) % 8 == 0, "FitDev is copied as 8-byte words");
 
     if (tid == 0) {
         for (int s = 0; s < n_stages; s++) {
             mbar_init(&full_bar[s], 1);
             mbar_init(&empty_bar[s], 1);
         }
+        mbar_init(&cnt_bar[0], 1);
+        mbar_init(&cnt_bar[1], 1);
         s_abort = 0;
     }
-    for (int k = tid; k < MC_MAX_PUB; k += blockDim.x) { pub_acc[k] = 0.0; pub_tile[k] = 0.0f; }
-    for (int k = tid; k < window_max * 2; k += blockDim.x) bins[k] = 0.0f;
+    for (int k = tid; k < MC_MAX_PUB; k += blockDim.x) { pub_acc[k] = 0.0; pub_tile[0][k] = 0.0f; pub_tile[1][k] = 0.0f; }
+    for (int k = tid; k < (int)(2 * L.bins_buf); k += blockDim.x) bins[k] = 0.0f;
     fence_async_shared();
     __syncthreads();
 
@@ -517,53 +555,86 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
         if (tid == nc) {
             int k = 0;
             int last_issued = -1;  // last ring slot k that received bulk copies
+            // The next tile's index and descriptor are fetched while the
+            // current one's copies are in flight.
+            int t_next = (int)atomicAdd(&ws->next_tile, 1u);
+            TileDev d_next{};
+            if (t_next < n_tiles) d_next = tiles[t_next];
+            int fit_cached = -1;
+            const unsigned char* f_tblk = nullptr;
+            const float* f_atr = nullptr;
+            const float* f_sat = nullptr;
             for (;; k++) {
                 int st = k % n_stages;
                 uint32_t round = (uint32_t)(k / n_stages);
-                if (!mbar_wait(&empty_bar[st], (round & 1u) ^ 1u, fits[0].status)) { s_abort = 1; break; }
-                int t = (int)atomicAdd(&ws->next_tile, 1u);
+                const int t = t_next;
+                const TileDev tile = d_next;
+                if (!mbar_wait(&empty_bar[st], (round & 1u) ^ 1u, status)) { s_abort = 1; break; }
                 if (t >= n_tiles || *(volatile int*)&s_abort) {
                     stage_tile[st] = -1;
                     mbar_arrive(&full_bar[st]);
                     break;
                 }
-                const TileDev tile = tiles[t];
-                const FitDev& f = fits[tile.fit];
                 stage_tile[st] = t;
+                stage_desc[st] = tile;
                 if (tile.qd_count > window_max) {  // direct tile: nothing to stage
                     mbar_arrive(&full_bar[st]);
-                    continue;
+                } else {
+                    if (tile.fit != fit_cached) {
+                        const FitDev& f = fits[tile.fit];
+                        f_tblk = reinterpret_cast<const unsigned char*>(f.tblk);
+                        f_atr = f.atr;
+                        f_sat = layout_stats(MODEL) > 1 ? f.sat : nullptr;
+                        fit_cached = tile.fit;
+                    }
+                    unsigned char* sb = smem + L.stage_off + (size_t)st * L.stage_bytes;
+                    int64_t a0 = tile.qd_begin & ~(int64_t)3;
+                    int64_t a1 = (tile.qd_begin + tile.qd_count + 3) & ~(int64_t)3;
+                    uint32_t wn = (uint32_t)(a1 - a0);
+                    uint32_t sess = 11u * (uint32_t)((tile.s_packed + 7) & ~7) * 2u;
+                    uint32_t bytes = sess + wn * 4 + (f_sat ? wn * 4 : 0);
+                    mbar_arrive_expect_tx(&full_bar[st], bytes);
+                    if (sess) bulk_g2s(sb, f_tblk + tile.blk_off, sess, &full_bar[st]);
+                    bulk_g2s(sb + L.atr_off, f_atr + a0, wn * 4, &full_bar[st]);
+                    if (f_sat) bulk_g2s(sb + L.sat_off, f_sat + a0, wn * 4, &full_bar[st]);
+                    last_issued = k;
                 }
-                unsigned char* sb = smem + L.stage_off + (size_t)st * L.stage_bytes;
-                int64_t a0 = tile.qd_begin & ~(int64_t)3;
-                int64_t a1 = (tile.qd_begin + tile.qd_count + 3) & ~(int64_t)3;
-                uint32_t wn = (uint32_t)(a1 - a0);
-                uint32_t sess = 11u * (uint32_t)((tile.s_packed + 7) & ~7) * 2u;
-                uint32_t bytes = sess + wn * 4 + wn * 8 + (f.sat ? wn * 4 : 0);
-                mbar_arrive_expect_tx(&full_bar[st], bytes);
-                if (sess) bulk_g2s(sb, reinterpret_cast<const unsigned char*>(f.tblk) + tile.blk_off, sess, &full_bar[st]);
-                bulk_g2s(sb + L.atr_off, f.atr + a0, wn * 4, &full_bar[st]);
-                if (f.sat) bulk_g2s(sb + L.sat_off, f.sat + a0, wn * 4, &full_bar[st]);
-                bulk_g2s(sb + L.cnt_off, f.cnt + a0, wn * 8, &full_bar[st]);
-                last_issued = k;
+                t_next = (int)atomicAdd(&ws->next_tile, 1u);
+                if (t_next < n_tiles) d_next = tiles[t_next];
             }
             // On a stop, wait (bounded) until every copy this warp issued into
             // the ring has landed, so none is still writing shared memory when
             // the CTA exits.
             if (*(volatile int*)&s_abort) {
                 for (int j = last_issued - n_stages + 1; j <= last_issued; j++)
-                    if (j >= 0) mbar_wait(&full_bar[j % n_stages], (uint32_t)(j / n_stages) & 1u, fits[0].status);
+                    if (j >= 0) mbar_wait(&full_bar[j % n_stages], (uint32_t)(j / n_stages) & 1u, status);
             }
         }
     } else {
         // ---------------- consumer warps ---------------------------------------
+        // Iteration k runs, as one pool of warp-sized items taken from a shared
+        // counter, the E-step of the k-th tile (bins buffer k & 1) and the
+        // M-step of the (k-1)-th tile (buffer (k-1) & 1, complete since the
+        // barrier that ended iteration k-1).  An M-step needs only its bins and
+        // the click counts in global memory, so the k-th tile's stage is
+        // released at the barrier that ends iteration k.  Tile and fit
+        // descriptors are read from shared memory (stage_desc -> s_desc,
+        // s_fit), never from global memory inside the loop.
         const int ctid = tid;
         const int lane = tid & 31;
+        const int warp = tid >> 5;
         int cur_fit = -1;
         unsigned cur_count = 0;
+        int prev_t = -1;
+        int fs = 0, pfs = 0;  // s_fit slots of the current fit and of the previous tile's fit
 
-        auto flush_fit = [&](int fit_id, unsigned count) {
-            const FitDev& f = fits[fit_id];
+        auto fold_pub = [&](int buf, const FitDev& f) {  // warp 0: a tile's FP32 partial into FP64
+            for (int q = lane; q < 2 * f.n_pub; q += 32) {
+                pub_acc[q] += (double)pub_tile[buf][q];
+                pub_tile[buf][q] = 0.0f;
+            }
+        };
+        auto flush_fit = [&](const FitDev& f, unsigned count) {
             consumer_sync(nc);
             for (int k = ctid; k < 2 * f.n_pub; k += nc) {
                 double v = pub_acc[k];
@@ -583,33 +654,143 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             }
             consumer_sync(nc);
         };
+        auto next_chunk = [&]() {
+            int c = 0;
+            if (lane == 0) c = atomicAdd(&s_chunk, 1);
+            return __shfl_sync(FULL_MASK, c, 0);
+        };
 
         for (int k = 0;; k++) {
-            int st = k % n_stages;
-            uint32_t round = (uint32_t)(k / n_stages);
+            const int st = k % n_stages;
+            const uint32_t round = (uint32_t)(k / n_stages);
             // Every consumer thread observes the completed phase itself.
-            if (!mbar_wait(&full_bar[st], round & 1u, fits[0].status)) s_abort = 1;
-            if (ctid == 0) s_chunk = 0;
+            if (!mbar_wait(&full_bar[st], round & 1u, status)) s_abort = 1;
+            if (ctid == 0) {
+                s_chunk = 0;
+                s_desc[k & 1] = stage_desc[st];  // slot k & 1 last held tile k - 2, done
+            }
             consumer_sync(nc);
-            if (*(volatile int*)&s_abort) break;
+            if (*(volatile int*)&s_abort) {
+                // The previous tile's count copy may still be in flight.
+                if (ctid == 0 && prev_t >= 0) mbar_wait(&cnt_bar[(k - 1) & 1], ((uint32_t)(k - 1) >> 1) & 1u, status);
+                break;
+            }
             const int t = stage_tile[st];
-            if (t < 0) break;
-            const TileDev tile = tiles[t];
-            const FitDev& f = fits[tile.fit];
-            if (tile.fit != cur_fit) {
-                if (cur_fit >= 0) flush_fit(cur_fit, cur_count);
+            TileDev tile{};
+            if (t >= 0) tile = s_desc[k & 1];
+            TileDev ptile{};
+            if (prev_t >= 0) ptile = s_desc[(k - 1) & 1];
+
+            // ---- public partial of the previous tile; fit changes -------------
+            bool folded = prev_t < 0;
+            if (t >= 0 && tile.fit != cur_fit) {
+                if (cur_fit >= 0) {
+                    if (warp == 0 && !folded) fold_pub((k - 1) & 1, s_fit[fs]);
+                    folded = true;
+                    flush_fit(s_fit[fs], cur_count);
+                    fs ^= 1;  // the other slot's fit has no tile left in flight
+                }
                 cur_fit = tile.fit;
                 cur_count = 0;
+                if (ctid < (int)(sizeof(FitDev) / 8))
+                    reinterpret_cast<uint64_t*>(&s_fit[fs])[ctid] = reinterpret_cast<const uint64_t*>(fits + cur_fit)[ctid];
                 // Public values are fixed for the whole launch of a fit.
-                int it = *(volatile int*)f.iter;
-                for (int q = ctid; q < f.n_pub; q += nc) pub_th[q] = f.pub_theta[(it & 1) * MC_MAX_PUB + q];
+                const FitDev& fg = fits[cur_fit];
+                int it = *(volatile int*)fg.iter;
+                for (int q = ctid; q < fg.n_pub; q += nc) pub_th[q] = fg.pub_theta[(it & 1) * MC_MAX_PUB + q];
                 consumer_sync(nc);
             }
-            const int model = model_of<MODEL>(f);
-            const int ns = private_stats(model);
-            const int n_pub = f.n_pub;
+            if (warp == 0 && !folded) fold_pub((k - 1) & 1, s_fit[pfs]);
+            // Click counts of this tile's window for its M-step (next
+            // iteration) into count slot k & 1, free since the M-step of tile
+            // k - 2 ended with the last barrier.  Every tile advances the
+            // slot's barrier by one phase, with or without a copy.
+            if (ctid == 0 && t >= 0) {
+                if (tile.split < 0) {
+                    const int64_t c0 = tile.qd_begin & ~(int64_t)3;
+                    const uint32_t cwn = (uint32_t)(((tile.qd_begin + tile.qd_count + 3) & ~(int64_t)3) - c0);
+                    fence_async_shared();
+                    mbar_arrive_expect_tx(&cnt_bar[k & 1], cwn * 4);
+                    bulk_g2s(cnt_slots + (k & 1) * L.cnt_slot, s_fit[fs].cnt16 + c0, cwn * 4, &cnt_bar[k & 1]);
+                } else {
+                    mbar_arrive(&cnt_bar[k & 1]);
+                }
+            }
 
-            const bool direct = tile.qd_count > window_max;
+            // ---- the pool: E-step chunks of tile t, then M-step items of prev_t -
+            const bool direct = t >= 0 && tile.qd_count > window_max;
+            const int n_sess = t < 0 ? 0 : (direct ? tile.s_count : tile.s_packed);
+            const int nE = (n_sess + 31) >> 5;
+            const int nM = prev_t < 0 ? 0 : (ptile.split >= 0 ? 1 : (ptile.qd_count + 63) >> 6);
+            if (prev_t >= 0 && ptile.split < 0 &&
+                !mbar_wait(&cnt_bar[(k - 1) & 1], ((uint32_t)(k - 1) >> 1) & 1u, status))
+                s_abort = 1;  // counts unreliable; the status word already says so
+            const uint32_t* cnt_m = cnt_slots + ((k - 1) & 1) * L.cnt_slot + (ptile.qd_begin & 3);
+            const int total = nE + nM;
+            float* bins_e = bins + (k & 1) * L.bins_buf;
+            float* bins_m = bins + ((k - 1) & 1) * L.bins_buf;
+            float* pub_k = pub_tile[k & 1];
+
+            // M-step items of the previous tile.  Owned tile: 64 qd per item,
+            // straight from the bins and the counts, written in place.  Split
+            // tile: one item, the warp folds the bins into the query's FP64
+            // bins and, if its tile is the query's last, runs the query's M-step.
+            auto mstep_item = [&](int mi) {
+                const FitDev& pf = s_fit[pfs];
+                const int pmodel = model_of<MODEL>(pf);
+                const int pns = private_stats(pmodel);
+                if (ptile.split < 0) {
+                    const int i0 = (mi << 6) + lane, i1 = i0 + 32;
+                    const bool h0 = i0 < ptile.qd_count, h1 = i1 < ptile.qd_count;
+                    const uint32_t p0 = h0 ? cnt_m[i0] : 0u, p1 = h1 ? cnt_m[i1] : 0u;
+                    const uint2 c0 = make_uint2(p0 & 0xFFFFu, p0 >> 16), c1 = make_uint2(p1 & 0xFFFFu, p1 >> 16);
+                    if (h0) {
+                        float v0 = bins_m[i0], v1 = 0.0f;
+                        bins_m[i0] = 0.0f;
+                        if (pns > 1) { v1 = bins_m[L.bins_stride + i0]; bins_m[L.bins_stride + i0] = 0.0f; }
+                        const int64_t q = ptile.qd_begin + i0;
+                        mstep_qd_f(pmodel, pf.mode, c0, v0, v1, pf.atr + q, pns > 1 ? pf.sat + q : nullptr);
+                    }
+                    if (h1) {
+                        float v0 = bins_m[i1], v1 = 0.0f;
+                        bins_m[i1] = 0.0f;
+                        if (pns > 1) { v1 = bins_m[L.bins_stride + i1]; bins_m[L.bins_stride + i1] = 0.0f; }
+                        const int64_t q = ptile.qd_begin + i1;
+                        mstep_qd_f(pmodel, pf.mode, c1, v0, v1, pf.atr + q, pns > 1 ? pf.sat + q : nullptr);
+                    }
+                    return;
+                }
+                const SplitDev sp = splits[ptile.split];
+                double* gb = pf.split_bins + sp.bin_offset;
+                if (ptile.qd_count <= window_max) {
+                    for (int i = lane; i < ptile.qd_count; i += 32)
+                        for (int kk = 0; kk < pns; kk++) {
+                            float v = bins_m[kk * L.bins_stride + i];
+                            if (v != 0.0f) { atomicAdd(gb + (int64_t)i * pns + kk, (double)v); bins_m[kk * L.bins_stride + i] = 0.0f; }
+                        }
+                }
+                __threadfence();
+                __syncwarp();
+                unsigned last = 0;
+                if (lane == 0) last = atomicAdd(pf.split_count + sp.local, 1u) + 1 == (unsigned)sp.n_tiles;
+                last = __shfl_sync(FULL_MASK, last, 0);
+                if (last) {
+                    __threadfence();
+                    for (int i = lane; i < sp.qd_count; i += 32) {
+                        int64_t q = sp.qd_begin + i;
+                        uint2 cn = __ldg(pf.cnt + q);
+                        double v0 = ld_cg(gb + (int64_t)i * pns);
+                        double v1 = pns > 1 ? ld_cg(gb + (int64_t)i * pns + 1) : 0.0;
+                        mstep_qd_d(pmodel, pf.mode, cn, v0, v1, pf.atr + q, pns > 1 ? pf.sat + q : nullptr);
+                        gb[(int64_t)i * pns] = 0.0;
+                        if (pns > 1) gb[(int64_t)i * pns + 1] = 0.0;
+                    }
+                    if (lane == 0) pf.split_count[sp.local] = 0;
+                }
+            };
+
+            const FitDev& f = s_fit[fs];
+            const int model = t >= 0 ? model_of<MODEL>(f) : -1;
             const unsigned char* sb = smem + L.stage_off + (size_t)st * L.stage_bytes;
             const int64_t a0 = tile.qd_begin & ~(int64_t)3;
             SmemSrc ssrc;
@@ -619,131 +800,85 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             ssrc.atr = reinterpret_cast<const float*>(sb + L.atr_off);
             ssrc.sat = reinterpret_cast<const float*>(sb + L.sat_off);
             ssrc.woff = (int)(tile.qd_begin - a0);
-            const uint2* cnt_w = reinterpret_cast<const uint2*>(sb + L.cnt_off) + ssrc.woff;
             GlobSrc gsrc;
             gsrc.pidx = f.pidx; gsrc.clk = f.click; gsrc.atr = f.atr; gsrc.sat = f.sat;
             gsrc.stride = f.stride; gsrc.s_begin = tile.s_begin; gsrc.qd_begin = tile.qd_begin;
             gsrc.qd_count = tile.qd_count; gsrc.status = f.status;
-            SmemSink ssink{bins, ns};
-            GlobSink gsink{tile.split >= 0 ? f.split_bins + splits[tile.split].bin_offset : nullptr, ns};
+            SmemSink ssink{bins_e, (int)L.bins_stride};
+            GlobSink gsink{direct ? f.split_bins + splits[tile.split].bin_offset : nullptr,
+                           t >= 0 ? private_stats(model) : 1};
 
-            // ---- E-step: warps take 32-session chunks from a shared counter --
-            // Staged tiles hold only the sessions that carry variable statistics
-            // (pack_tiles_kernel); direct tiles read every session.
-            const int n_sess = direct ? tile.s_count : tile.s_packed;
-            const int n_chunks = (n_sess + 31) >> 5;
-            auto next_chunk = [&]() {
-                int c = 0;
-                if (lane == 0) c = atomicAdd(&s_chunk, 1);
-                return __shfl_sync(FULL_MASK, c, 0);
+            // E-step chunks first (the long dependency chains start early);
+            // M-step items fill in behind them.
+            auto run_pool = [&](auto&& echunk) {
+                for (int c = next_chunk(); c < total; c = next_chunk()) {
+                    if (c < nE) echunk((c << 5) + lane);
+                    else mstep_item(c - nE);
+                }
             };
             if (model == PBM) {
                 float acc[MC_R];
 #pragma unroll
                 for (int r = 0; r < MC_R; r++) acc[r] = 0.0f;
-                for (int c = next_chunk(); c < n_chunks; c = next_chunk()) {
-                    int sl = (c << 5) + lane;
+                run_pool([&](int sl) {
                     if (sl < n_sess) {
                         if (direct) estep_pbm(gsrc, gsink, sl, pub_th, acc);
                         else estep_pbm(ssrc, ssink, sl, pub_th, acc);
                     }
-                }
+                });
 #pragma unroll
                 for (int r = 0; r < MC_R; r++) {
                     float v = warp_sum(acc[r]);
-                    if (lane == 0 && v != 0.0f) atomicAdd(pub_tile + 2 * r, v);
+                    if (lane == 0 && v != 0.0f) atomicAdd(pub_k + 2 * r, v);
                 }
             } else if (model == UBM) {
-                for (int c = next_chunk(); c < n_chunks; c = next_chunk()) {
-                    int sl = (c << 5) + lane;
+                run_pool([&](int sl) {
                     int key[MC_R];
                     float var[MC_R];
                     if (direct) estep_ubm(gsrc, gsink, sl, sl < n_sess, pub_th, key, var);
                     else estep_ubm(ssrc, ssink, sl, sl < n_sess, pub_th, key, var);
-                    reduce_ubm_public(key, var, pub_tile);
-                }
+                    reduce_ubm_public(key, var, pub_k);
+                });
             } else if (model == DBN) {
                 float gn = 0.0f, gd = 0.0f;
                 const float g = pub_th[0];
-                for (int c = next_chunk(); c < n_chunks; c = next_chunk()) {
-                    int sl = (c << 5) + lane;
+                run_pool([&](int sl) {
                     if (sl < n_sess) {
                         if (direct) estep_dbn(gsrc, gsink, sl, g, gn, gd);
                         else estep_dbn(ssrc, ssink, sl, g, gn, gd);
                     }
-                }
+                });
                 gn = warp_sum(gn);
                 gd = warp_sum(gd);
-                if (lane == 0) { atomicAdd(pub_tile + 0, gn); atomicAdd(pub_tile + 1, gd); }
-            } else {
+                if (lane == 0) { atomicAdd(pub_k + 0, gn); atomicAdd(pub_k + 1, gd); }
+            } else if (model == CCM) {
                 float tt[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
                 const float t1 = pub_th[0], t2 = pub_th[1], t3 = pub_th[2];
-                for (int c = next_chunk(); c < n_chunks; c = next_chunk()) {
-                    int sl = (c << 5) + lane;
+                run_pool([&](int sl) {
                     if (sl < n_sess) {
                         if (direct) estep_ccm(gsrc, gsink, sl, t1, t2, t3, tt);
                         else estep_ccm(ssrc, ssink, sl, t1, t2, t3, tt);
                     }
-                }
+                });
 #pragma unroll
                 for (int q = 0; q < 6; q++) {
                     float v = warp_sum(tt[q]);
-                    if (lane == 0) atomicAdd(pub_tile + q, v);
-                }
-            }
-            consumer_sync(nc);
-
-            // ---- M-step of the window ------------------------------------------
-            if (tile.split < 0) {
-                for (int i = ctid; i < tile.qd_count; i += nc) {
-                    int64_t q = tile.qd_begin + i;
-                    float v0 = bins[i * ns];
-                    float v1 = ns > 1 ? bins[i * ns + 1] : 0.0f;
-                    bins[i * ns] = 0.0f;
-                    if (ns > 1) bins[i * ns + 1] = 0.0f;
-                    mstep_qd_f(model, f.mode, cnt_w[i], v0, v1, f.atr + q, ns > 1 ? f.sat + q : nullptr);
+                    if (lane == 0) atomicAdd(pub_k + q, v);
                 }
             } else {
-                const SplitDev sp = splits[tile.split];
-                double* gb = f.split_bins + sp.bin_offset;
-                if (!direct) {
-                    for (int i = ctid; i < tile.qd_count * ns; i += nc) {
-                        float v = bins[i];
-                        if (v != 0.0f) { atomicAdd(gb + i, (double)v); bins[i] = 0.0f; }
-                    }
-                }
-                __threadfence();
-                consumer_sync(nc);
-                if (ctid == 0) {
-                    unsigned old = atomicAdd(f.split_count + sp.local, 1u);
-                    s_last = (old + 1 == (unsigned)sp.n_tiles);
-                }
-                consumer_sync(nc);
-                if (s_last) {
-                    __threadfence();
-                    for (int i = ctid; i < sp.qd_count; i += nc) {
-                        int64_t q = sp.qd_begin + i;
-                        uint2 cn = __ldg(f.cnt + q);
-                        double v0 = ld_cg(gb + (int64_t)i * ns);
-                        double v1 = ns > 1 ? ld_cg(gb + (int64_t)i * ns + 1) : 0.0;
-                        mstep_qd_d(model, f.mode, cn, v0, v1, f.atr + q, ns > 1 ? f.sat + q : nullptr);
-                        gb[(int64_t)i * ns] = 0.0;
-                        if (ns > 1) gb[(int64_t)i * ns + 1] = 0.0;
-                    }
-                    if (ctid == 0) f.split_count[sp.local] = 0;
-                }
+                run_pool([&](int) {});
             }
-
-            // ---- fold the tile's public partial; release the stage ---------------
-            for (int q = ctid; q < 2 * n_pub; q += nc) {
-                pub_acc[q] += (double)pub_tile[q];
-                pub_tile[q] = 0.0f;
-            }
-            cur_count++;
+            // A direct tile's statistics went to global memory: order them
+            // before the barrier, after which the split counter is raised.
+            if (direct) __threadfence();
             consumer_sync(nc);
+            if (t < 0) break;
             if (ctid == 0) mbar_arrive(&empty_bar[st]);
+            prev_t = t;
+            pfs = fs;
+            cur_count++;
         }
-        if (cur_fit >= 0 && !s_abort) flush_fit(cur_fit, cur_count);
+        if (cur_fit >= 0 && !*(volatile int*)&s_abort) flush_fit(s_fit[fs], cur_count);
     }
     __syncthreads();
     if (tid == 0) {
@@ -754,12 +889,10 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             ws->ctas_exited = 0;
         }
     }
-    (void)status_any;
 }
 
 size_t fused_smem_bytes(int model, int window_max, int spt, int n_stages) {
-    (void)model;
-    Layout L = make_layout(spt, window_max);
+    Layout L = make_layout(model, spt, window_max);
     return (size_t)L.stage_off + (size_t)n_stages * L.stage_bytes;
 }
 

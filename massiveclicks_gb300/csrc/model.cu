@@ -143,6 +143,15 @@ __global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32
 }
 
 // The plain path's 8-byte rank-major records, built from the planes.
+// Click counts as 16-bit pairs for the fused M-step of whole-query tiles.
+__global__ void pack_counts_kernel(const uint2* __restrict__ cnt, uint32_t* __restrict__ cnt16, int64_t n) {
+    const int64_t step = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
+        const uint2 c = cnt[i];
+        cnt16[i] = (c.x < 65535u ? c.x : 65535u) | ((c.y < 65535u ? c.y : 65535u) << 16);
+    }
+}
+
 __global__ void build_recs_kernel(int64_t n, int64_t stride, const int32_t* planes, const uint16_t* click, PlainRec* recs) {
     int64_t step = (int64_t)gridDim.x * blockDim.x;
     for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += step) {
@@ -177,6 +186,7 @@ struct mc_model {
     int32_t* d_pidx = nullptr;
     uint16_t* d_click = nullptr;
     uint2* d_cnt = nullptr;
+    uint32_t* d_cnt16 = nullptr;
     float *d_atr = nullptr, *d_sat = nullptr, *d_pub_theta = nullptr;
     double *d_pub_bins = nullptr, *d_pub_const = nullptr, *d_split_bins = nullptr;
     unsigned *d_split_count = nullptr, *d_tiles_done = nullptr;
@@ -245,7 +255,7 @@ struct mc_model {
         drop_graph();
         free_tiles();
         free_plain();
-        dfree(d_pidx); dfree(d_click); dfree(d_cnt); dfree(d_atr); dfree(d_sat); dfree(d_pub_theta);
+        dfree(d_pidx); dfree(d_click); dfree(d_cnt); dfree(d_cnt16); dfree(d_atr); dfree(d_sat); dfree(d_pub_theta);
         dfree(d_pub_bins); dfree(d_pub_const); dfree(d_tiles_done); dfree(d_iter); dfree(d_status);
         dfree(d_fit); dfree(d_ws); dfree(d_grad);
         bytes = test_bytes;
@@ -400,6 +410,7 @@ FitDev mc_model::make_desc() const {
     f.pidx = d_pidx;
     f.click = d_click;
     f.cnt = d_cnt;
+    f.cnt16 = d_cnt16;
     f.tblk = d_tblk;
     f.atr = d_atr;
     f.sat = d_sat;
@@ -497,6 +508,7 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     // aligned bulk copies of any window stay inside the allocation.
     const int64_t qd_alloc = m->qd_alloc();
     if ((rc = dalloc(&m->d_cnt, (size_t)qd_alloc, &B))) return rc;
+    if ((rc = dalloc(&m->d_cnt16, (size_t)qd_alloc, &B))) return rc;
     if ((rc = dalloc(&m->d_atr, (size_t)qd_alloc, &B))) return rc;
     if (m->model == MC_DBN && (rc = dalloc(&m->d_sat, (size_t)qd_alloc, &B))) return rc;
     if ((rc = dalloc(&m->d_pub_theta, 2 * MC_MAX_PUB, &B))) return rc;
@@ -541,6 +553,11 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
         int grid = (int)std::min<int64_t>((n + 255) / 256, (int64_t)8 * m->n_sm);
         prep_kernel<<<grid, 256, 0, st>>>(n, m->stride, n_qd, d_src, m->d_click, d_seg_begin, n_seg, m->model,
                                           m->d_pidx, m->d_cnt, d_seg_lo, d_seg_hi, d_pub_counts, d_flag);
+        ck(cudaGetLastError());
+    }
+    {
+        int grid = (int)std::min<int64_t>((qd_alloc + 255) / 256, (int64_t)8 * m->n_sm);
+        pack_counts_kernel<<<grid, 256, 0, st>>>(m->d_cnt, m->d_cnt16, qd_alloc);
         ck(cudaGetLastError());
     }
     int flag = 0;

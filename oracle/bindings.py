@@ -39,6 +39,7 @@ def load() -> C.CDLL:
     lib.orc_fit_new.restype = vp
     lib.orc_fit_new.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, vp, vp, vp, C.c_int64]
     lib.orc_fit_run.argtypes = [vp, C.c_int, C.c_int]
+    lib.orc_fit_set_copies.argtypes = [vp, C.c_int]
     lib.orc_fit_n_params.restype = C.c_int64
     lib.orc_fit_n_params.argtypes = [vp]
     lib.orc_fit_get.argtypes = [vp, vp, vp, vp]
@@ -101,7 +102,10 @@ class OracleFit:
         self.h = self.lib.orc_fit_new(0 if dtype == "f32" else 1, model, mode, self._q.shape[0], _p(self._q),
                                       _p(self._p), _p(self._m), self.n_qd)
 
-    def run(self, iterations: int, threads: int = 1) -> None:
+    def run(self, iterations: int, threads: int = 1, copy_sessions: bool = True) -> None:
+        """copy_sessions=False skips the reference's per-thread dataset copies
+        of DBN/CCM (same results, less time and memory)."""
+        self.lib.orc_fit_set_copies(self.h, int(bool(copy_sessions)))
         self.lib.orc_fit_run(self.h, int(iterations), int(threads))
 
     def flat(self):

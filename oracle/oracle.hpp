@@ -27,7 +27,8 @@
 // The per-thread copy of the whole training set that the reference's DBN and
 // CCM E-step threads receive (dbn.cu:244, ccm.cu:223: std::thread copies its
 // by-value argument) is reproduced in multi-threaded runs, since it is part of
-// what the CPU baseline costs.
+// what the CPU baseline costs; copy_sessions = false leaves it out where
+// only the results matter (the copies do not change them).
 #ifndef MCLICKS_ORACLE_HPP
 #define MCLICKS_ORACLE_HPP
 
@@ -175,6 +176,7 @@ static const int kFactorInputs[8][3] = {{0, 0, 0}, {0, 0, 1}, {0, 1, 0}, {0, 1, 
 template <typename T>
 struct Fit {
     int type = PBM, mode = PARITY;
+    bool copy_sessions = true;  // per-thread dataset copies of DBN/CCM (baseline timing only)
     int64_t n = 0, n_qd = 0;
     std::vector<Param<T>> atr, sat, pub;          // pub: exm (10 / 55), gamma (1), tau (3)
     std::vector<Param<T>> atr_tmp, sat_tmp, pub_tmp;
@@ -426,7 +428,7 @@ struct Fit {
         std::vector<std::thread> pool;
         for (int t = 0; t < threads; t++) {
             int64_t e = b + (t < left ? part + 1 : part);
-            if (type == DBN || type == CCM) {
+            if ((type == DBN || type == CCM) && copy_sessions) {
                 // The reference hands each thread its own copy of the sessions.
                 pool.emplace_back([this, b, e](std::vector<Session> copy) { estep_range(copy, b, e); }, data);
             } else {

@@ -233,6 +233,12 @@ int orc_fit_run(void* h, int iterations, int threads) {
     return 0;
 }
 
+void orc_fit_set_copies(void* h, int copy_sessions) {
+    FitBox* b = (FitBox*)h;
+    b->f32.copy_sessions = copy_sessions != 0;
+    b->f64.copy_sessions = copy_sessions != 0;
+}
+
 int64_t orc_fit_n_params(void* h) {
     FitBox* b = (FitBox*)h;
     if (b->dtype == 0) return (int64_t)(b->f32.atr.size() + b->f32.sat.size() + b->f32.pub.size());

@@ -60,7 +60,11 @@ def test_batch_equals_separate_fits(config):
         cm.em(7)
     for (model, train, n_qd), bm, sm in zip(parts, batch_models, single_models):
         got, alone = bm.get_parameters(), sm.get_parameters()
-        _close(got, {k: v.astype(np.float64) for k, v in alone.items()}, 1e-6, 1e-7, f"batch vs alone m{model}")
+        # Shared-memory FP32 bins are summed in a run-dependent order, so two
+        # runs of the same fit differ by a few ulp per iteration (~1e-6 after
+        # 7 iterations); statistics lost or mixed between fits would show as
+        # errors of 1e-3 and more.
+        _close(got, {k: v.astype(np.float64) for k, v in alone.items()}, 5e-6, 1e-6, f"batch vs alone m{model}")
         f = bindings.OracleFit("f64", model, 0, train.query, train.pidx, train.click, n_qd)
         f.run(7)
         _close(got, f.values(), PARAM_RTOL, PARAM_ATOL, f"batch vs oracle m{model}")

@@ -1,0 +1,89 @@
+"""Precision study on sessions shaped like the 20M-session CCM-click workload
+(Zipf(1.0) queries, 50-doc pools, top-10 shown, ground-truth CCM clicks with
+tau = 0.6 / 0.3 / 0.2 and relevance ~ Beta(1, 3)).  DBN and CCM are fitted for
+50 iterations from the prior by
+
+  * fused: FP32 E-step with per-rank scaling, FP32 shared-memory bins per
+    tile, FP64 fold for split queries and public statistics;
+  * plain: FP32 E-step in log space, FP32 global atomics (all-FP32);
+  * the FP64 oracle: the reference's CPU path in double precision;
+
+and each GPU variant's parameter max-abs error and test log-likelihood and
+perplexity errors against the oracle are printed (one JSON line per model,
+prefixed PRECISION) and, if MC_PRECISION_OUT names a file, appended to it.
+
+Default size 2M sessions over 100k queries; MC_PRECISION_SESSIONS=20000000
+runs the full 20M sessions over 1M queries (the FP64 oracle then needs several
+minutes of host time per model)."""
+import json
+import os
+import time
+
+import numpy as np
+import pytest
+
+from massiveclicks_gb300 import api
+from massiveclicks_gb300._capi import IMPL_FUSED, IMPL_PLAIN
+from oracle import bindings
+
+pytestmark = pytest.mark.gpu
+
+ITERATIONS = 50
+TEST_LL_RTOL = 1e-5
+
+
+def _errors(got: dict, ref: dict) -> dict:
+    out = {}
+    for k, r in ref.items():
+        g = got[k].astype(np.float64)
+        err = np.abs(g - r)
+        out[k] = {"max_abs": float(err.max()), "max_rel": float((err / np.maximum(np.abs(r), 1e-30)).max())}
+    return out
+
+
+@pytest.fixture(scope="module")
+def dataset():
+    n = int(os.environ.get("MC_PRECISION_SESSIONS", "2000000"))
+    cfg = api.synth_config(2, n_sessions=n, n_queries=max(1000, n // 20))
+    q, d, m = api.synth_sessions(cfg)
+    return api.Dataset.from_sessions(q, d, m, 0.2), n
+
+
+@pytest.mark.parametrize("model", [api.DBN, api.CCM])
+def test_precision_against_fp64_oracle(dataset, model):
+    ds, n = dataset
+    runs = {}
+    for name, impl in (("fused", IMPL_FUSED), ("plain", IMPL_PLAIN)):
+        cm = api.ClickModel.create(model)
+        cm.init_parameters(ds)
+        t0 = time.perf_counter()
+        cm.em(ITERATIONS, impl)
+        ev = cm.evaluate(1)
+        runs[name] = (cm.get_parameters(), ev, time.perf_counter() - t0)
+        cm.destroy_parameters()
+
+    f = bindings.OracleFit("f64", model, 0, ds.train.query, ds.train.pidx, ds.train.click, ds.n_qd)
+    t0 = time.perf_counter()
+    f.run(ITERATIONS, threads=os.cpu_count() or 1, copy_sessions=False)
+    t_oracle = time.perf_counter() - t0
+    ref = f.values()
+    ref_ev = f.evaluate(ds.test.pidx, ds.test.click)
+
+    line = {"model": {api.DBN: "DBN", api.CCM: "CCM"}[model], "sessions": n, "train_sessions": len(ds.train),
+            "n_qd": ds.n_qd, "iterations": ITERATIONS,
+            "oracle": {"test_llh": ref_ev["llh"], "perplexity": ref_ev["ppl"], "seconds": t_oracle}}
+    for name, (params, ev, secs) in runs.items():
+        line[name] = {"params": _errors(params, ref),
+                      "test_llh": ev.llh, "test_llh_rel_err": abs(ev.llh - ref_ev["llh"]) / abs(ref_ev["llh"]),
+                      "perplexity": ev.perplexity,
+                      "perplexity_rel_err": abs(ev.perplexity - ref_ev["ppl"]) / ref_ev["ppl"],
+                      "seconds_incl_eval": secs}
+    print("PRECISION " + json.dumps(line))
+    out = os.environ.get("MC_PRECISION_OUT")
+    if out:
+        with open(out, "a") as fh:
+            fh.write(json.dumps(line) + "\n")
+    # The product path carries the parity bar; the plain all-FP32 variant is
+    # reported, not held to it.
+    assert line["fused"]["test_llh_rel_err"] <= TEST_LL_RTOL
+    assert line["fused"]["perplexity_rel_err"] <= TEST_LL_RTOL
