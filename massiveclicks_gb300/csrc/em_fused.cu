@@ -3,26 +3,27 @@
 //
 // Work: a queue of session tiles (host-built, see model.cu).  Each tile is a
 // run of whole queries (or a chunk of one large query) whose qd indices form
-// one contiguous window.  Persistent CTAs (two per SM):
-//   * a producer warp takes the next tile from the global queue and issues
-//     bulk async copies (cp.async.bulk, completion on an mbarrier) of the tile's
-//     packed sessions (uint16 window-relative indices, rank-major, and click
-//     masks) and of the window's parameter values into a ring of
-//     shared-memory stages;
-//   * consumer warps wait on the stage's mbarrier; then, as one pool of
-//     warp-sized items taken from a shared counter, they run the E-step of
-//     that tile (one thread per session, entirely from shared memory, each
-//     private statistic added into a shared-memory bin per qd, each public one
-//     into registers) and the M-step of the tile before it, whose bins are in
-//     the other of two bin buffers:
+// one contiguous window.  Persistent CTAs (two per SM), every warp a worker:
+//   * thread 0 keeps a ring of shared-memory stages filled: for the next tile
+//     from the global queue it issues bulk async copies (cp.async.bulk,
+//     completion on an mbarrier) of the tile's packed sessions (uint16
+//     window-relative indices, rank-major, and click masks) and of the
+//     window's parameter values; a stage is refilled right after the tile
+//     that used it is done, with a tile index fetched one iteration ahead;
+//   * the warps wait on the stage's mbarrier; then, as one pool of warp-sized
+//     items taken from a shared counter, they run the E-step of that tile
+//     (one thread per session, entirely from shared memory, each private
+//     statistic added into a shared-memory bin per qd, each public one into
+//     registers) and the M-step of the tile before it, whose bins are in the
+//     other of two bin buffers:
 //       - owned tile (whole queries): M-step for the window straight from the
-//         bins and the click counts, written in place to global memory (no
-//         other tile reads those parameters);
+//         bins and the click counts (copied into shared memory one tile
+//         ahead), written in place to global memory (no other tile reads
+//         those parameters);
 //       - split tile (part of a large query): one warp folds the bins into the
 //         query's FP64 global bins, and the warp that completes the query's
 //         last tile runs its M-step;
-//     one barrier ends the item pool, and the stage goes back to the producer
-//     (second mbarrier).
+//     one barrier ends the item pool and frees the tile's stage.
 //   * public statistics: warp shuffles -> shared FP32 partial per tile -> FP64
 //     per-CTA accumulator -> one FP64 global atomic per bin per CTA; the CTA
 //     that completes the fit's last tile runs the public M-step into the other
@@ -394,10 +395,14 @@ __device__ __forceinline__ void estep_ccm(const Src& src, const Sink& sink, int 
             // depends on the parameters.  An unclicked rank adds exactly
             // (1, 1) to tau_1: a constant of the fit, added at upload.
             if ((m >> r) & 1u) {
+                // u = x / (x + y) and 1 - u = y / (x + y), each from its own
+                // numerator: 1 - u formed by subtraction loses the small
+                // tau_3 share to cancellation when tau_3 is near 0.
                 float x = ia * t2, y = a[r] * t3;
-                float u = __fdividef(x, x + y);
+                float inv = __fdividef(1.0f, x + y);
+                float u = x * inv, v = y * inv;
                 t[2] += u; t[3] += u;
-                t[4] += 1.0f - u; t[5] += 1.0f - u;
+                t[4] += v; t[5] += v;
             }
         } else if (r == l) {
             float k2 = 1.0f - t2 * (1.0f - R), k3 = 1.0f - t3 * (1.0f - R);
@@ -520,27 +525,23 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
     __shared__ double pub_acc[MC_MAX_PUB];
     __shared__ float pub_tile[2][MC_MAX_PUB];
     __shared__ float pub_th[MC_MAX_PUB];
-    __shared__ __align__(8) uint64_t full_bar[FUSED_MAX_STAGES], empty_bar[FUSED_MAX_STAGES], cnt_bar[2];
+    __shared__ __align__(8) uint64_t full_bar[FUSED_MAX_STAGES], cnt_bar[2];
     __shared__ int stage_tile[FUSED_MAX_STAGES];
-    __shared__ TileDev stage_desc[FUSED_MAX_STAGES];   // the staged tile's descriptor (producer)
-    __shared__ TileDev s_desc[2];                      // consumers: the k-th tile's descriptor in slot k & 1
-    __shared__ __align__(16) FitDev s_fit[2];          // consumers: current fit and the one before
+    __shared__ TileDev stage_desc[FUSED_MAX_STAGES];   // the staged tile's descriptor
+    __shared__ TileDev s_desc[2];                      // the k-th tile's descriptor in slot k & 1
+    __shared__ __align__(16) FitDev s_fit[2];          // current fit and the one before
     __shared__ int s_last, s_it, s_abort, s_chunk;
 
     const Layout L = make_layout(MODEL, spt, window_max);
     float* bins = reinterpret_cast<float*>(smem);
     uint32_t* cnt_slots = reinterpret_cast<uint32_t*>(smem + L.cnt_off);
     const int tid = threadIdx.x;
-    const int nc = blockDim.x - 32;            // consumer threads; the last warp produces
-    const bool producer = tid >= nc;
+    const int nc = blockDim.x;  // every warp takes work items
     int* const status = fits[0].status;
     static_assert(sizeof(FitDev) % 8 == 0, "FitDev is copied as 8-byte words");
 
     if (tid == 0) {
-        for (int s = 0; s < n_stages; s++) {
-            mbar_init(&full_bar[s], 1);
-            mbar_init(&empty_bar[s], 1);
-        }
+        for (int s = 0; s < n_stages; s++) mbar_init(&full_bar[s], 1);
         mbar_init(&cnt_bar[0], 1);
         mbar_init(&cnt_bar[1], 1);
         s_abort = 0;
@@ -550,68 +551,48 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
     fence_async_shared();
     __syncthreads();
 
-    if (producer) {
-        // ---------------- producer warp ----------------------------------------
-        if (tid == nc) {
-            int k = 0;
-            int last_issued = -1;  // last ring slot k that received bulk copies
-            // The next tile's index and descriptor are fetched while the
-            // current one's copies are in flight.
-            int t_next = (int)atomicAdd(&ws->next_tile, 1u);
-            TileDev d_next{};
-            if (t_next < n_tiles) d_next = tiles[t_next];
-            int fit_cached = -1;
-            const unsigned char* f_tblk = nullptr;
-            const float* f_atr = nullptr;
-            const float* f_sat = nullptr;
-            for (;; k++) {
-                int st = k % n_stages;
-                uint32_t round = (uint32_t)(k / n_stages);
-                const int t = t_next;
-                const TileDev tile = d_next;
-                if (!mbar_wait(&empty_bar[st], (round & 1u) ^ 1u, status)) { s_abort = 1; break; }
-                if (t >= n_tiles || *(volatile int*)&s_abort) {
-                    stage_tile[st] = -1;
-                    mbar_arrive(&full_bar[st]);
-                    break;
-                }
-                stage_tile[st] = t;
-                stage_desc[st] = tile;
-                if (tile.qd_count > window_max) {  // direct tile: nothing to stage
-                    mbar_arrive(&full_bar[st]);
-                } else {
-                    if (tile.fit != fit_cached) {
-                        const FitDev& f = fits[tile.fit];
-                        f_tblk = reinterpret_cast<const unsigned char*>(f.tblk);
-                        f_atr = f.atr;
-                        f_sat = layout_stats(MODEL) > 1 ? f.sat : nullptr;
-                        fit_cached = tile.fit;
-                    }
-                    unsigned char* sb = smem + L.stage_off + (size_t)st * L.stage_bytes;
-                    int64_t a0 = tile.qd_begin & ~(int64_t)3;
-                    int64_t a1 = (tile.qd_begin + tile.qd_count + 3) & ~(int64_t)3;
-                    uint32_t wn = (uint32_t)(a1 - a0);
-                    uint32_t sess = 11u * (uint32_t)((tile.s_packed + 7) & ~7) * 2u;
-                    uint32_t bytes = sess + wn * 4 + (f_sat ? wn * 4 : 0);
-                    mbar_arrive_expect_tx(&full_bar[st], bytes);
-                    if (sess) bulk_g2s(sb, f_tblk + tile.blk_off, sess, &full_bar[st]);
-                    bulk_g2s(sb + L.atr_off, f_atr + a0, wn * 4, &full_bar[st]);
-                    if (f_sat) bulk_g2s(sb + L.sat_off, f_sat + a0, wn * 4, &full_bar[st]);
-                    last_issued = k;
-                }
-                t_next = (int)atomicAdd(&ws->next_tile, 1u);
-                if (t_next < n_tiles) d_next = tiles[t_next];
-            }
-            // On a stop, wait (bounded) until every copy this warp issued into
-            // the ring has landed, so none is still writing shared memory when
-            // the CTA exits.
-            if (*(volatile int*)&s_abort) {
-                for (int j = last_issued - n_stages + 1; j <= last_issued; j++)
-                    if (j >= 0) mbar_wait(&full_bar[j % n_stages], (uint32_t)(j / n_stages) & 1u, status);
-            }
+    // Stage filling, by thread 0 only.  The j-th tile this CTA takes goes to
+    // stage j % n_stages: bulk copies of its packed sessions and of its
+    // window's values, completion on full_bar.  A stage is refilled at the
+    // start of the iteration after the one that used it (the barrier ending
+    // that iteration is the release), with a tile index fetched one
+    // iteration earlier, so the atomic's latency is off the critical path.
+    auto fill_stage = [&](int st, int t) {
+        fence_async_shared();  // generic reads of the old contents before the async writes
+        if (t >= n_tiles) {
+            stage_tile[st] = -1;
+            mbar_arrive(&full_bar[st]);
+            return;
         }
-    } else {
-        // ---------------- consumer warps ---------------------------------------
+        const TileDev tile = tiles[t];
+        stage_tile[st] = t;
+        stage_desc[st] = tile;
+        if (tile.qd_count > window_max) {  // direct tile: nothing to stage
+            mbar_arrive(&full_bar[st]);
+            return;
+        }
+        const FitDev& f = fits[tile.fit];
+        const float* f_sat = layout_stats(MODEL) > 1 ? f.sat : nullptr;
+        unsigned char* sb = smem + L.stage_off + (size_t)st * L.stage_bytes;
+        const int64_t a0 = tile.qd_begin & ~(int64_t)3;
+        const int64_t a1 = (tile.qd_begin + tile.qd_count + 3) & ~(int64_t)3;
+        const uint32_t wn = (uint32_t)(a1 - a0);
+        const uint32_t sess = 11u * (uint32_t)((tile.s_packed + 7) & ~7) * 2u;
+        mbar_arrive_expect_tx(&full_bar[st], sess + wn * 4 + (f_sat ? wn * 4 : 0));
+        if (sess) bulk_g2s(sb, reinterpret_cast<const unsigned char*>(f.tblk) + tile.blk_off, sess, &full_bar[st]);
+        bulk_g2s(sb + L.atr_off, f.atr + a0, wn * 4, &full_bar[st]);
+        if (f_sat) bulk_g2s(sb + L.sat_off, f_sat + a0, wn * 4, &full_bar[st]);
+    };
+    int t_pre = 0;   // thread 0: the next tile index, fetched an iteration ahead
+    int filled = 0;  // thread 0: stage fills issued so far
+    if (tid == 0) {
+        for (int s = 0; s < n_stages; s++) fill_stage(s, (int)atomicAdd(&ws->next_tile, 1u));
+        filled = n_stages;
+        t_pre = (int)atomicAdd(&ws->next_tile, 1u);
+    }
+
+    {
+        // ---------------- the tile loop ----------------------------------------
         // Iteration k runs, as one pool of warp-sized items taken from a shared
         // counter, the E-step of the k-th tile (bins buffer k & 1) and the
         // M-step of the (k-1)-th tile (buffer (k-1) & 1, complete since the
@@ -671,11 +652,21 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             }
             consumer_sync(nc);
             if (*(volatile int*)&s_abort) {
-                // The previous tile's count copy may still be in flight.
-                if (ctid == 0 && prev_t >= 0) mbar_wait(&cnt_bar[(k - 1) & 1], ((uint32_t)(k - 1) >> 1) & 1u, status);
+                // Copies this CTA issued may still be in flight: the previous
+                // tile's counts and the stages filled but not yet consumed.
+                if (ctid == 0) {
+                    if (prev_t >= 0) mbar_wait(&cnt_bar[(k - 1) & 1], ((uint32_t)(k - 1) >> 1) & 1u, status);
+                    for (int j = k; j < filled; j++)
+                        mbar_wait(&full_bar[j % n_stages], (uint32_t)(j / n_stages) & 1u, status);
+                }
                 break;
             }
             const int t = stage_tile[st];
+            if (ctid == 0 && k > 0) {
+                fill_stage((k - 1) % n_stages, t_pre);  // the (k - 1 + n_stages)-th tile
+                filled++;
+                t_pre = (int)atomicAdd(&ws->next_tile, 1u);
+            }
             TileDev tile{};
             if (t >= 0) tile = s_desc[k & 1];
             TileDev ptile{};
@@ -873,7 +864,6 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             if (direct) __threadfence();
             consumer_sync(nc);
             if (t < 0) break;
-            if (ctid == 0) mbar_arrive(&empty_bar[st]);
             prev_t = t;
             pfs = fs;
             cur_count++;
@@ -977,7 +967,12 @@ __global__ void pack_tiles_kernel(int model, TileDev* tiles, int n_tiles, int wi
         __syncthreads();
         atomicAdd(&s_kept, kept);
         __syncthreads();
-        const int n_kept = s_kept;
+        // The host sized the tile's block for tile.s_packed sessions.
+        int n_kept = s_kept;
+        if (n_kept > tile.s_packed) {
+            if (threadIdx.x == 0) atomicOr(status, ST_BAD_INDEX);
+            n_kept = tile.s_packed;
+        }
         const int spad = (n_kept + 7) & ~7;
         uint16_t* rel = reinterpret_cast<uint16_t*>(tblk + tile.blk_off);
         uint16_t* clk = rel + 10 * spad;
@@ -996,12 +991,12 @@ __global__ void pack_tiles_kernel(int model, TileDev* tiles, int n_tiles, int wi
     }
 }
 
-cudaError_t launch_pack_tiles(int model, TileDev* tiles, int n_tiles, int window_max, int spt, const int32_t* planes,
+cudaError_t launch_pack_tiles(int model, TileDev* tiles, int n_tiles, int window_max, int max_tile_sessions, const int32_t* planes,
                               int64_t stride, const uint16_t* click, unsigned char* tblk, int* status, int n_sm,
                               cudaStream_t st) {
     if (n_tiles == 0) return cudaSuccess;
     int P = 1;
-    while (P < spt) P <<= 1;
+    while (P < max_tile_sessions) P <<= 1;
     int g = n_tiles < 8 * n_sm ? n_tiles : 8 * n_sm;
     pack_tiles_kernel<<<g, 256, (size_t)P * 4, st>>>(model, tiles, n_tiles, window_max, planes, stride, click, tblk, status);
     return cudaGetLastError();

@@ -181,6 +181,7 @@ struct mc_model {
     std::string fused_reason;
     // query segments of the training set: sessions and qd range
     std::vector<int64_t> seg_begin, seg_lo, seg_hi;
+    std::vector<uint8_t> packable;  // DBN/CCM: 1 for a training session with a click
     int spt = 1024, wqd = 1536, block = 256, stages = 2, ctas_per_sm = 1;
     // fused state
     int32_t* d_pidx = nullptr;
@@ -282,13 +283,24 @@ struct mc_model {
     int ensure_plain(cudaStream_t st);
 };
 
-// Splits the query segments into tiles of at most `spt` sessions and `wqd`
-// qd per window.  A query above either bound becomes a split query: chunks of
-// at most `spt` sessions that share FP64 bins.
+// Bound on the sessions of one staged tile (its packing sort holds them all
+// in shared memory).
+static const int kTileSessions = 4096;
+
+// Splits the query segments into tiles.  A staged tile holds at most `spt`
+// packed sessions (those its E-step reads: for DBN and CCM the sessions with
+// a click, otherwise all), at most kTileSessions sessions in all, and a window
+// of at most `wqd` qd.  A query above a bound becomes a split query:
+// consecutive chunks that share FP64 bins, cut so that the chunks carry equal
+// numbers of packed sessions; a query whose window exceeds `wqd` is read
+// directly from global memory in chunks of at most `spt` sessions.
 int mc_model::build_tiles() {
     drop_graph();
     free_tiles();
     const int ns = private_stats(model);
+    const bool drop = (model == MC_DBN || model == MC_CCM) && packable.size() == (size_t)n;
+    auto packed_at = [&](int64_t s) -> int { return drop ? (int)packable[(size_t)s] : 1; };
+    const int64_t max_sess = std::max<int64_t>(spt, kTileSessions);
     std::vector<TileDev> tiles;
     std::vector<SplitDev> splits;
     int64_t bin_off = 0;
@@ -299,57 +311,90 @@ int mc_model::build_tiles() {
         if (open) tiles.push_back(cur);
         open = false;
     };
+    auto new_split = [&](int64_t lo, int64_t hi) {
+        SplitDev sp;
+        sp.qd_begin = lo;
+        sp.qd_count = (int)(hi - lo);
+        sp.n_tiles = 0;
+        sp.bin_offset = bin_off;
+        sp.local = (int)splits.size();
+        sp.pad_ = 0;
+        bin_off += (hi - lo) * ns;
+        splits.push_back(sp);
+        return (int)splits.size() - 1;
+    };
+    auto split_tile = [&](int sid, int64_t b, int64_t e, int pk) {
+        TileDev t{};
+        t.fit = 0;
+        t.split = sid;
+        t.s_begin = b;
+        t.s_count = (int)(e - b);
+        t.qd_begin = splits[(size_t)sid].qd_begin;
+        t.qd_count = splits[(size_t)sid].qd_count;
+        t.blk_off = 0;
+        t.s_packed = pk;
+        tiles.push_back(t);
+        splits[(size_t)sid].n_tiles++;
+    };
     for (size_t g = 0; g < n_seg; g++) {
-        int64_t sb = seg_begin[g], sc = seg_begin[g + 1] - sb;
-        int64_t lo = seg_lo[g], hi = seg_hi[g];
-        if (sc > spt || hi - lo > wqd) {
+        const int64_t sb = seg_begin[g], sc = seg_begin[g + 1] - sb;
+        const int64_t lo = seg_lo[g], hi = seg_hi[g];
+        if (hi - lo > wqd) {  // direct: every session read from global memory
             close();
-            int nt = (int)((sc + spt - 1) / spt);
-            SplitDev sp;
-            sp.qd_begin = lo;
-            sp.qd_count = (int)(hi - lo);
-            sp.n_tiles = nt;
-            sp.bin_offset = bin_off;
-            sp.local = (int)splits.size();
-            sp.pad_ = 0;
-            bin_off += (hi - lo) * ns;
-            int sid = (int)splits.size();
-            splits.push_back(sp);
-            for (int k = 0; k < nt; k++) {
-                int64_t b = sb + sc * k / nt, e = sb + sc * (k + 1) / nt;
-                TileDev t{};
-                t.fit = 0;
-                t.split = sid;
-                t.s_begin = b;
-                t.s_count = (int)(e - b);
-                t.qd_begin = lo;
-                t.qd_count = (int)(hi - lo);
-                t.blk_off = 0;
-                t.s_packed = t.s_count;
-                tiles.push_back(t);
+            const int sid = new_split(lo, hi);
+            const int64_t nt = (sc + spt - 1) / spt;
+            for (int64_t k = 0; k < nt; k++) {
+                const int64_t b = sb + sc * k / nt, e = sb + sc * (k + 1) / nt;
+                split_tile(sid, b, e, (int)(e - b));
             }
             continue;
         }
-        if (open && (cur.s_count + sc > spt || hi - cur.qd_begin > wqd)) close();
+        int64_t pk = 0;
+        for (int64_t s = sb; s < sb + sc; s++) pk += packed_at(s);
+        if (pk > spt || sc > max_sess) {  // staged split query
+            close();
+            const int sid = new_split(lo, hi);
+            const int64_t nt0 = std::max<int64_t>(1, (pk + spt - 1) / spt);
+            const int64_t target = std::max<int64_t>(1, (pk + nt0 - 1) / nt0);
+            int64_t b = sb;
+            int tpk = 0;
+            for (int64_t s = sb; s < sb + sc; s++) {
+                tpk += packed_at(s);
+                if ((tpk == target || s + 1 - b == max_sess) && s + 1 < sb + sc) {
+                    split_tile(sid, b, s + 1, tpk);
+                    b = s + 1;
+                    tpk = 0;
+                }
+            }
+            split_tile(sid, b, sb + sc, tpk);
+            continue;
+        }
+        if (open && (cur.s_packed + pk > spt || cur.s_count + sc > max_sess || hi - cur.qd_begin > wqd)) close();
         if (!open) {
             cur = TileDev{};
             cur.fit = 0;
             cur.split = -1;
             cur.s_begin = sb;
             cur.s_count = 0;
+            cur.s_packed = 0;
             cur.qd_begin = lo;
             open = true;
         }
         cur.s_count += (int)sc;
-        cur.s_packed = cur.s_count;
+        cur.s_packed += (int)pk;
         cur.qd_count = (int)(hi - cur.qd_begin);
     }
     close();
     // Packed session blocks of the staged (non-direct) tiles, 16-byte aligned.
+    // Sized by the packed counts, which the packing kernel checks.
     int64_t blk = 0;
+    int max_tile_sessions = 1;
     for (TileDev& t : tiles) {
         t.blk_off = blk;
-        if (t.qd_count <= wqd) blk += 22 * (int64_t)((t.s_count + 7) & ~7);
+        if (t.qd_count <= wqd) {
+            blk += 22 * (int64_t)((t.s_packed + 7) & ~7);
+            max_tile_sessions = std::max(max_tile_sessions, t.s_count);
+        }
     }
     n_tiles = (int)tiles.size();
     n_splits = (int)splits.size();
@@ -390,7 +435,7 @@ int mc_model::build_tiles() {
     grid = std::max(1, std::min(n_tiles, ctas_per_sm * n_sm));
     int rc2 = write_fit_desc();
     if (rc2) return rc2;
-    CK(launch_pack_tiles(model, d_tiles, n_tiles, wqd, spt, d_pidx, stride, d_click, d_tblk, d_status, n_sm, 0));
+    CK(launch_pack_tiles(model, d_tiles, n_tiles, wqd, max_tile_sessions, d_pidx, stride, d_click, d_tblk, d_status, n_sm, 0));
     CK(cudaDeviceSynchronize());
     int status = 0;
     CK(cudaMemcpy(&status, d_status, 4, cudaMemcpyDeviceToHost));
@@ -499,6 +544,11 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
         if (s == 0 || query[s] != query[s - 1]) m->seg_begin.push_back(s);
     const int64_t n_seg = (int64_t)m->seg_begin.size();
     m->seg_begin.push_back(n);
+    m->packable.clear();
+    if (m->model == MC_DBN || m->model == MC_CCM) {
+        m->packable.resize((size_t)n);
+        for (int64_t s = 0; s < n; s++) m->packable[(size_t)s] = click[s] != 0;
+    }
 
     int rc;
     int64_t& B = m->bytes;
