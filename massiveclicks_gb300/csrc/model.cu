@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -78,7 +79,7 @@ __global__ void pairs_to_pub_kernel(const float2* pub2, float* theta, const int*
 __global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32_t* __restrict__ pidx_sm,
                             const uint16_t* __restrict__ click, const int64_t* __restrict__ seg_begin, int64_t n_seg,
                             int model, int32_t* planes, uint2* cnt, int* seg_lo, int* seg_hi,
-                            unsigned long long* pub_counts, int* flag) {
+                            unsigned long long* pub_counts, uint32_t* packbits, int* flag) {
     __shared__ unsigned int sc[MC_PUB_COUNTS];
     for (int k = threadIdx.x; k < MC_PUB_COUNTS; k += blockDim.x) sc[k] = 0;
     __syncthreads();
@@ -89,8 +90,12 @@ __global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32
         bool valid = s < n;
         int lo = INT_MAX, hi = INT_MIN;
         int64_t seg = -1;
+        const unsigned m = valid ? click[s] : 0u;
+        // Bit s of packbits: session s has a click (32 consecutive sessions per warp).
+        const unsigned word = __ballot_sync(0xffffffffu, m != 0u);
+        const int64_t w0 = s0 + (threadIdx.x & ~31);  // first session of this warp, a multiple of 32
+        if ((threadIdx.x & 31) == 0 && w0 < n) packbits[w0 >> 5] = word;
         if (valid) {
-            unsigned m = click[s];
             int64_t a = 0, b = n_seg - 1;  // last segment with begin <= s
             while (a < b) {
                 int64_t mid = (a + b + 1) / 2;
@@ -181,7 +186,7 @@ struct mc_model {
     std::string fused_reason;
     // query segments of the training set: sessions and qd range
     std::vector<int64_t> seg_begin, seg_lo, seg_hi;
-    std::vector<uint8_t> packable;  // DBN/CCM: 1 for a training session with a click
+    std::vector<uint32_t> packbits;  // bit s: training session s has a click
     int spt = 1024, wqd = 1536, block = 256, stages = 2, ctas_per_sm = 1;
     // fused state
     int32_t* d_pidx = nullptr;
@@ -298,8 +303,21 @@ int mc_model::build_tiles() {
     drop_graph();
     free_tiles();
     const int ns = private_stats(model);
-    const bool drop = (model == MC_DBN || model == MC_CCM) && packable.size() == (size_t)n;
-    auto packed_at = [&](int64_t s) -> int { return drop ? (int)packable[(size_t)s] : 1; };
+    const bool drop = (model == MC_DBN || model == MC_CCM) && packbits.size() == (size_t)((n + 31) / 32);
+    auto packed_at = [&](int64_t s) -> int { return drop ? (int)((packbits[(size_t)(s >> 5)] >> (s & 31)) & 1u) : 1; };
+    // Packed sessions in [b, e): popcounts of the covered words, the two end
+    // words masked.
+    auto packed_in = [&](int64_t b, int64_t e) -> int64_t {
+        if (!drop) return e - b;
+        if (b >= e) return 0;
+        const int64_t wb = b >> 5, we = (e - 1) >> 5;
+        const uint32_t head = 0xFFFFFFFFu << (b & 31);
+        const uint32_t tail = (e & 31) ? (0xFFFFFFFFu >> (32 - (e & 31))) : 0xFFFFFFFFu;
+        if (wb == we) return __builtin_popcount(packbits[(size_t)wb] & head & tail);
+        int64_t c = __builtin_popcount(packbits[(size_t)wb] & head) + __builtin_popcount(packbits[(size_t)we] & tail);
+        for (int64_t w = wb + 1; w < we; w++) c += __builtin_popcount(packbits[(size_t)w]);
+        return c;
+    };
     const int64_t max_sess = std::max<int64_t>(spt, kTileSessions);
     std::vector<TileDev> tiles;
     std::vector<SplitDev> splits;
@@ -349,24 +367,34 @@ int mc_model::build_tiles() {
             }
             continue;
         }
-        int64_t pk = 0;
-        for (int64_t s = sb; s < sb + sc; s++) pk += packed_at(s);
+        const int64_t pk = packed_in(sb, sb + sc);
         if (pk > spt || sc > max_sess) {  // staged split query
             close();
             const int sid = new_split(lo, hi);
             const int64_t nt0 = std::max<int64_t>(1, (pk + spt - 1) / spt);
             const int64_t target = std::max<int64_t>(1, (pk + nt0 - 1) / nt0);
+            const int64_t e = sb + sc;
             int64_t b = sb;
             int tpk = 0;
-            for (int64_t s = sb; s < sb + sc; s++) {
+            for (int64_t s = sb; s < e;) {
+                // A whole aligned word that reaches neither bound is taken at once.
+                if ((s & 31) == 0 && s + 32 <= e) {
+                    const int w = drop ? __builtin_popcount(packbits[(size_t)(s >> 5)]) : 32;
+                    if (tpk + w < target && s + 32 - b < max_sess) {
+                        tpk += w;
+                        s += 32;
+                        continue;
+                    }
+                }
                 tpk += packed_at(s);
-                if ((tpk == target || s + 1 - b == max_sess) && s + 1 < sb + sc) {
+                if ((tpk == target || s + 1 - b == max_sess) && s + 1 < e) {
                     split_tile(sid, b, s + 1, tpk);
                     b = s + 1;
                     tpk = 0;
                 }
+                s++;
             }
-            split_tile(sid, b, sb + sc, tpk);
+            split_tile(sid, b, e, tpk);
             continue;
         }
         if (open && (cur.s_packed + pk > spt || cur.s_count + sc > max_sess || hi - cur.qd_begin > wqd)) close();
@@ -538,17 +566,26 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     m->n_qd = n_qd;
     m->stride = std::max<int64_t>(32, (n + 31) / 32 * 32);
 
-    // Query segments (runs of equal query id).
+    // Query segments (runs of equal query id), scanned by several host
+    // threads over contiguous ranges.
     m->seg_begin.clear();
-    for (int64_t s = 0; s < n; s++)
-        if (s == 0 || query[s] != query[s - 1]) m->seg_begin.push_back(s);
+    {
+        const int nth = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::thread::hardware_concurrency(), n / (1 << 20)));
+        std::vector<std::vector<int64_t>> part((size_t)nth);
+        auto scan = [&](int t) {
+            const int64_t b = n * t / nth, e = n * (t + 1) / nth;
+            for (int64_t s = b; s < e; s++)
+                if (s == 0 || query[s] != query[s - 1]) part[(size_t)t].push_back(s);
+        };
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nth; t++) pool.emplace_back(scan, t);
+        scan(0);
+        for (auto& th : pool) th.join();
+        for (auto& v : part) m->seg_begin.insert(m->seg_begin.end(), v.begin(), v.end());
+    }
     const int64_t n_seg = (int64_t)m->seg_begin.size();
     m->seg_begin.push_back(n);
-    m->packable.clear();
-    if (m->model == MC_DBN || m->model == MC_CCM) {
-        m->packable.resize((size_t)n);
-        for (int64_t s = 0; s < n; s++) m->packable[(size_t)s] = click[s] != 0;
-    }
+
 
     int rc;
     int64_t& B = m->bytes;
@@ -575,13 +612,16 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     int64_t* d_seg_begin = nullptr;
     int *d_seg_lo = nullptr, *d_seg_hi = nullptr, *d_flag = nullptr;
     unsigned long long* d_pub_counts = nullptr;
+    uint32_t* d_packbits = nullptr;
+    const int64_t n_words = (n + 31) / 32;
     int64_t scratch = 0;
-    auto free_scratch = [&]() { dfree(d_src); dfree(d_seg_begin); dfree(d_seg_lo); dfree(d_seg_hi); dfree(d_flag); dfree(d_pub_counts); };
+    auto free_scratch = [&]() { dfree(d_src); dfree(d_seg_begin); dfree(d_seg_lo); dfree(d_seg_hi); dfree(d_flag); dfree(d_pub_counts); dfree(d_packbits); };
     if ((rc = dalloc(&d_src, (size_t)std::max<int64_t>(n * MC_R, 1), &scratch)) ||
         (rc = dalloc(&d_seg_begin, (size_t)(n_seg + 1), &scratch)) ||
         (rc = dalloc(&d_seg_lo, (size_t)std::max<int64_t>(n_seg, 1), &scratch)) ||
         (rc = dalloc(&d_seg_hi, (size_t)std::max<int64_t>(n_seg, 1), &scratch)) ||
-        (rc = dalloc(&d_flag, 1, &scratch)) || (rc = dalloc(&d_pub_counts, MC_PUB_COUNTS, &scratch))) {
+        (rc = dalloc(&d_flag, 1, &scratch)) || (rc = dalloc(&d_pub_counts, MC_PUB_COUNTS, &scratch)) ||
+        (rc = dalloc(&d_packbits, (size_t)std::max<int64_t>(n_words, 1), &scratch))) {
         free_scratch();
         return rc;
     }
@@ -602,7 +642,7 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     if (n && e == cudaSuccess) {
         int grid = (int)std::min<int64_t>((n + 255) / 256, (int64_t)8 * m->n_sm);
         prep_kernel<<<grid, 256, 0, st>>>(n, m->stride, n_qd, d_src, m->d_click, d_seg_begin, n_seg, m->model,
-                                          m->d_pidx, m->d_cnt, d_seg_lo, d_seg_hi, d_pub_counts, d_flag);
+                                          m->d_pidx, m->d_cnt, d_seg_lo, d_seg_hi, d_pub_counts, d_packbits, d_flag);
         ck(cudaGetLastError());
     }
     {
@@ -615,6 +655,8 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     std::vector<int> lo(init_lo.size()), hi(init_hi.size());
     ck(cudaMemcpyAsync(&flag, d_flag, 4, cudaMemcpyDeviceToHost, st));
     ck(cudaMemcpyAsync(pub_counts.data(), d_pub_counts, pub_counts.size() * 8, cudaMemcpyDeviceToHost, st));
+    m->packbits.assign((size_t)n_words, 0u);
+    if (n_words) ck(cudaMemcpyAsync(m->packbits.data(), d_packbits, (size_t)n_words * 4, cudaMemcpyDeviceToHost, st));
     ck(cudaMemcpyAsync(lo.data(), d_seg_lo, lo.size() * 4, cudaMemcpyDeviceToHost, st));
     ck(cudaMemcpyAsync(hi.data(), d_seg_hi, hi.size() * 4, cudaMemcpyDeviceToHost, st));
     ck(cudaStreamSynchronize(st));
@@ -711,9 +753,12 @@ extern "C" int mc_model_configure(mc_model* m, int32_t spt, int32_t wqd, int32_t
     if (spt && spt > 4096) return set_error(MC_ERR_INVALID, "model_configure: sessions per tile above 4096");
     wqd = (wqd + 7) & ~7;
     CK(cudaSetDevice(m->device));
+    const int spt0 = m->spt, wqd0 = m->wqd, block0 = m->block;
     if (spt) m->spt = spt;
     if (wqd) m->wqd = wqd;
     if (block) m->block = block;
+    // Unchanged shape: the tiles, occupancy and graphs stay valid.
+    if (m->spt == spt0 && m->wqd == wqd0 && m->block == block0) return MC_OK;
     if (m->uploaded && m->fused_ok) return m->build_tiles();
     return MC_OK;
 }
