@@ -291,12 +291,18 @@ def run_ours(args, rank: int, world: int, local: int):
     design_bytes = 22 * n_clicked + 24 * n_qd
     tr = profile_traffic()
     traffic = None
+    traffic_source = None
     if tr and tr.get("bytes_per_launch") and tr.get("n_train") and tr.get("n_qd"):
-        # scaled from the profiled case by the bytes model 42 B/session + 24 B/qd
-        scale = (42 * n_train + 24 * n_qd) / (42 * tr["n_train"] + 24 * tr["n_qd"])
-        traffic = tr["bytes_per_launch"] * scale
+        if tr["n_train"] == n_train and tr["n_qd"] == n_qd:
+            traffic = tr["bytes_per_launch"]
+            traffic_source = "ncu dram__bytes_read.sum + dram__bytes_write.sum, this workload"
+        else:
+            # scaled from the profiled case by the bytes model 42 B/session + 24 B/qd
+            scale = (42 * n_train + 24 * n_qd) / (42 * tr["n_train"] + 24 * tr["n_qd"])
+            traffic = tr["bytes_per_launch"] * scale
+            traffic_source = f"ncu capture of {tr['n_train']} training sessions, scaled"
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": traffic,
+                "traffic": traffic, "traffic_source": traffic_source,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks.get("hbm_gbs") else "fallback 6.8 TB/s",
                 "algorithmic_bytes_per_launch": algo_bytes,
                 "bytes_model": "42 B/session + 80 B/qd (DBN; survey hot-path table)",
