@@ -77,7 +77,7 @@ __global__ void pairs_to_pub_kernel(const float2* pub2, float* theta, const int*
 // qd range of each query segment, and the click counts behind the public
 // constants (PBM: clicks per rank; UBM: written and clicked-written slots).
 __global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32_t* __restrict__ pidx_sm,
-                            const uint16_t* __restrict__ click, const int64_t* __restrict__ seg_begin, int64_t n_seg,
+                            const uint16_t* __restrict__ click, const int32_t* __restrict__ seg_id,
                             int model, int32_t* planes, uint2* cnt, int* seg_lo, int* seg_hi,
                             unsigned long long* pub_counts, uint32_t* packbits, int* flag) {
     __shared__ unsigned int sc[MC_PUB_COUNTS];
@@ -96,12 +96,7 @@ __global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32
         const int64_t w0 = s0 + (threadIdx.x & ~31);  // first session of this warp, a multiple of 32
         if ((threadIdx.x & 31) == 0 && w0 < n) packbits[w0 >> 5] = word;
         if (valid) {
-            int64_t a = 0, b = n_seg - 1;  // last segment with begin <= s
-            while (a < b) {
-                int64_t mid = (a + b + 1) / 2;
-                if (seg_begin[mid] <= s) a = mid; else b = mid - 1;
-            }
-            seg = a;
+            seg = seg_id[s];
             int last = 9, slot[MC_R];
 #pragma unroll
             for (int r = 0; r < MC_R; r++) {
@@ -148,6 +143,66 @@ __global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32
 }
 
 // The plain path's 8-byte rank-major records, built from the planes.
+// Query segments on the device.  Block b covers sessions [b * 2048, (b + 1) * 2048),
+// eight consecutive sessions per thread; a session starts a segment when its
+// query differs from the previous session's.
+constexpr int kSegBlock = 2048;
+
+__global__ void seg_count_kernel(int64_t n, const int32_t* __restrict__ query, int* __restrict__ blk_count) {
+    __shared__ int warp_sum[8];
+    const int64_t base = (int64_t)blockIdx.x * kSegBlock + (int64_t)threadIdx.x * 8;
+    int c = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int64_t s = base + k;
+        if (s < n) c += (s == 0 || query[s] != query[s - 1]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < 8; w++) t += warp_sum[w];
+        blk_count[blockIdx.x] = t;
+    }
+}
+
+// Writes seg_begin[] (the first session of every segment, in order) and the
+// segment index of every session; blk_off[b] is the number of segments that
+// start before block b.
+__global__ void seg_write_kernel(int64_t n, const int32_t* __restrict__ query, const int64_t* __restrict__ blk_off,
+                                 int64_t* __restrict__ seg_begin, int32_t* __restrict__ seg_id) {
+    __shared__ int warp_sum[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t base = (int64_t)blockIdx.x * kSegBlock + (int64_t)threadIdx.x * 8;
+    unsigned flags = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int64_t s = base + k;
+        if (s < n && (s == 0 || query[s] != query[s - 1])) flags |= 1u << k;
+    }
+    const int c = __popc(flags);
+    int incl = c;  // inclusive scan over the lanes
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) warp_sum[warp] = incl;
+    __syncthreads();
+    int before = 0;
+    for (int w = 0; w < warp; w++) before += warp_sum[w];
+    int64_t idx = blk_off[blockIdx.x] + before + incl - c;  // segments starting before this thread's first session
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int64_t s = base + k;
+        if (s >= n) break;
+        if ((flags >> k) & 1u) seg_begin[idx++] = s;
+        seg_id[s] = (int32_t)(idx - 1);
+    }
+}
+
 // Click counts as 16-bit pairs for the fused M-step of whole-query tiles.
 __global__ void pack_counts_kernel(const uint2* __restrict__ cnt, uint32_t* __restrict__ cnt16, int64_t n) {
     const int64_t step = (int64_t)gridDim.x * blockDim.x;
@@ -566,58 +621,84 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     m->n_qd = n_qd;
     m->stride = std::max<int64_t>(32, (n + 31) / 32 * 32);
 
-    // Query segments (runs of equal query id), scanned by several host
-    // threads over contiguous ranges.
-    m->seg_begin.clear();
+    // Query segments (runs of equal query id), found on the device: block
+    // counts, their prefix on the host, then seg_begin and each session's
+    // segment index.
+    int32_t* d_q = nullptr;
+    int32_t* d_seg_id = nullptr;
+    int64_t* d_seg_begin = nullptr;
+    int64_t n_seg = 0;
     {
-        const int nth = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::thread::hardware_concurrency(), n / (1 << 20)));
-        std::vector<std::vector<int64_t>> part((size_t)nth);
-        auto scan = [&](int t) {
-            const int64_t b = n * t / nth, e = n * (t + 1) / nth;
-            for (int64_t s = b; s < e; s++)
-                if (s == 0 || query[s] != query[s - 1]) part[(size_t)t].push_back(s);
-        };
-        std::vector<std::thread> pool;
-        for (int t = 1; t < nth; t++) pool.emplace_back(scan, t);
-        scan(0);
-        for (auto& th : pool) th.join();
-        for (auto& v : part) m->seg_begin.insert(m->seg_begin.end(), v.begin(), v.end());
+        int64_t scratch0 = 0;
+        const int64_t nb = (n + kSegBlock - 1) / kSegBlock;
+        int* d_blk = nullptr;
+        int64_t* d_off = nullptr;
+        int rc0;
+        auto free0 = [&]() { dfree(d_blk); dfree(d_off); };
+        if ((rc0 = dalloc(&d_q, (size_t)std::max<int64_t>(n, 1), &scratch0)) ||
+            (rc0 = dalloc(&d_seg_id, (size_t)std::max<int64_t>(n, 1), &scratch0)) ||
+            (rc0 = dalloc(&d_blk, (size_t)std::max<int64_t>(nb, 1), &scratch0)) ||
+            (rc0 = dalloc(&d_off, (size_t)std::max<int64_t>(nb, 1), &scratch0))) {
+            free0(); dfree(d_q); dfree(d_seg_id);
+            return rc0;
+        }
+        std::vector<int> blk((size_t)nb);
+        std::vector<int64_t> off((size_t)nb);
+        cudaError_t e0 = cudaSuccess;
+        auto ck0 = [&](cudaError_t x) { if (e0 == cudaSuccess) e0 = x; };
+        if (n) {
+            ck0(cudaMemcpyAsync(d_q, query, (size_t)n * 4, cudaMemcpyHostToDevice, st));
+            seg_count_kernel<<<(unsigned)nb, kSegBlock / 8, 0, st>>>(n, d_q, d_blk);
+            ck0(cudaGetLastError());
+            ck0(cudaMemcpyAsync(blk.data(), d_blk, (size_t)nb * 4, cudaMemcpyDeviceToHost, st));
+            ck0(cudaStreamSynchronize(st));
+            for (int64_t b = 0; b < nb; b++) { off[(size_t)b] = n_seg; n_seg += blk[(size_t)b]; }
+            if (e0 == cudaSuccess && (rc0 = dalloc(&d_seg_begin, (size_t)std::max<int64_t>(n_seg, 1), &scratch0))) {
+                free0(); dfree(d_q); dfree(d_seg_id);
+                return rc0;
+            }
+            ck0(cudaMemcpyAsync(d_off, off.data(), (size_t)nb * 8, cudaMemcpyHostToDevice, st));
+            seg_write_kernel<<<(unsigned)nb, kSegBlock / 8, 0, st>>>(n, d_q, d_off, d_seg_begin, d_seg_id);
+            ck0(cudaGetLastError());
+        }
+        m->seg_begin.assign((size_t)n_seg + 1, n);
+        if (n_seg) ck0(cudaMemcpyAsync(m->seg_begin.data(), d_seg_begin, (size_t)n_seg * 8, cudaMemcpyDeviceToHost, st));
+        ck0(cudaStreamSynchronize(st));
+        free0();
+        dfree(d_q);
+        if (e0 != cudaSuccess) { dfree(d_seg_id); dfree(d_seg_begin); return cuda_fail("model_upload", e0); }
     }
-    const int64_t n_seg = (int64_t)m->seg_begin.size();
-    m->seg_begin.push_back(n);
-
 
     int rc;
     int64_t& B = m->bytes;
-    if ((rc = dalloc(&m->d_pidx, (size_t)(m->stride * MC_R), &B))) return rc;
-    if ((rc = dalloc(&m->d_click, (size_t)std::max<int64_t>(n, 1), &B))) return rc;
+    auto fail_seg = [&](int code) { dfree(d_seg_id); dfree(d_seg_begin); return code; };
+    if ((rc = dalloc(&m->d_pidx, (size_t)(m->stride * MC_R), &B))) return fail_seg(rc);
+    if ((rc = dalloc(&m->d_click, (size_t)std::max<int64_t>(n, 1), &B))) return fail_seg(rc);
     // Parameter arrays padded to a multiple of 4 entries plus 4, so 16-byte
     // aligned bulk copies of any window stay inside the allocation.
     const int64_t qd_alloc = m->qd_alloc();
-    if ((rc = dalloc(&m->d_cnt, (size_t)qd_alloc, &B))) return rc;
-    if ((rc = dalloc(&m->d_cnt16, (size_t)qd_alloc, &B))) return rc;
-    if ((rc = dalloc(&m->d_atr, (size_t)qd_alloc, &B))) return rc;
-    if (m->model == MC_DBN && (rc = dalloc(&m->d_sat, (size_t)qd_alloc, &B))) return rc;
-    if ((rc = dalloc(&m->d_pub_theta, 2 * MC_MAX_PUB, &B))) return rc;
-    if ((rc = dalloc(&m->d_pub_bins, (size_t)(2 * m->n_pub), &B))) return rc;
-    if ((rc = dalloc(&m->d_pub_const, (size_t)(2 * m->n_pub), &B))) return rc;
-    if ((rc = dalloc(&m->d_tiles_done, 1, &B))) return rc;
-    if ((rc = dalloc(&m->d_iter, 1, &B))) return rc;
-    if ((rc = dalloc(&m->d_status, 1, &B))) return rc;
-    if ((rc = dalloc(&m->d_fit, 1, &B))) return rc;
-    if ((rc = dalloc(&m->d_ws, 1, &B))) return rc;
+    if ((rc = dalloc(&m->d_cnt, (size_t)qd_alloc, &B))) return fail_seg(rc);
+    if ((rc = dalloc(&m->d_cnt16, (size_t)qd_alloc, &B))) return fail_seg(rc);
+    if ((rc = dalloc(&m->d_atr, (size_t)qd_alloc, &B))) return fail_seg(rc);
+    if (m->model == MC_DBN && (rc = dalloc(&m->d_sat, (size_t)qd_alloc, &B))) return fail_seg(rc);
+    if ((rc = dalloc(&m->d_pub_theta, 2 * MC_MAX_PUB, &B))) return fail_seg(rc);
+    if ((rc = dalloc(&m->d_pub_bins, (size_t)(2 * m->n_pub), &B))) return fail_seg(rc);
+    if ((rc = dalloc(&m->d_pub_const, (size_t)(2 * m->n_pub), &B))) return fail_seg(rc);
+    if ((rc = dalloc(&m->d_tiles_done, 1, &B))) return fail_seg(rc);
+    if ((rc = dalloc(&m->d_iter, 1, &B))) return fail_seg(rc);
+    if ((rc = dalloc(&m->d_status, 1, &B))) return fail_seg(rc);
+    if ((rc = dalloc(&m->d_fit, 1, &B))) return fail_seg(rc);
+    if ((rc = dalloc(&m->d_ws, 1, &B))) return fail_seg(rc);
 
     // Scratch for the preparation pass.
     int32_t* d_src = nullptr;
-    int64_t* d_seg_begin = nullptr;
     int *d_seg_lo = nullptr, *d_seg_hi = nullptr, *d_flag = nullptr;
     unsigned long long* d_pub_counts = nullptr;
     uint32_t* d_packbits = nullptr;
     const int64_t n_words = (n + 31) / 32;
     int64_t scratch = 0;
-    auto free_scratch = [&]() { dfree(d_src); dfree(d_seg_begin); dfree(d_seg_lo); dfree(d_seg_hi); dfree(d_flag); dfree(d_pub_counts); dfree(d_packbits); };
+    auto free_scratch = [&]() { dfree(d_src); dfree(d_seg_begin); dfree(d_seg_id); dfree(d_seg_lo); dfree(d_seg_hi); dfree(d_flag); dfree(d_pub_counts); dfree(d_packbits); };
     if ((rc = dalloc(&d_src, (size_t)std::max<int64_t>(n * MC_R, 1), &scratch)) ||
-        (rc = dalloc(&d_seg_begin, (size_t)(n_seg + 1), &scratch)) ||
         (rc = dalloc(&d_seg_lo, (size_t)std::max<int64_t>(n_seg, 1), &scratch)) ||
         (rc = dalloc(&d_seg_hi, (size_t)std::max<int64_t>(n_seg, 1), &scratch)) ||
         (rc = dalloc(&d_flag, 1, &scratch)) || (rc = dalloc(&d_pub_counts, MC_PUB_COUNTS, &scratch)) ||
@@ -632,7 +713,6 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
         ck(cudaMemcpyAsync(d_src, pidx, (size_t)n * MC_R * 4, cudaMemcpyHostToDevice, st));
         ck(cudaMemcpyAsync(m->d_click, click, (size_t)n * 2, cudaMemcpyHostToDevice, st));
     }
-    ck(cudaMemcpyAsync(d_seg_begin, m->seg_begin.data(), (size_t)(n_seg + 1) * 8, cudaMemcpyHostToDevice, st));
     ck(cudaMemcpyAsync(d_seg_lo, init_lo.data(), init_lo.size() * 4, cudaMemcpyHostToDevice, st));
     ck(cudaMemcpyAsync(d_seg_hi, init_hi.data(), init_hi.size() * 4, cudaMemcpyHostToDevice, st));
     ck(cudaMemsetAsync(d_flag, 0, 4, st));
@@ -641,7 +721,7 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     ck(cudaMemsetAsync(m->d_cnt, 0, (size_t)qd_alloc * sizeof(uint2), st));
     if (n && e == cudaSuccess) {
         int grid = (int)std::min<int64_t>((n + 255) / 256, (int64_t)8 * m->n_sm);
-        prep_kernel<<<grid, 256, 0, st>>>(n, m->stride, n_qd, d_src, m->d_click, d_seg_begin, n_seg, m->model,
+        prep_kernel<<<grid, 256, 0, st>>>(n, m->stride, n_qd, d_src, m->d_click, d_seg_id, m->model,
                                           m->d_pidx, m->d_cnt, d_seg_lo, d_seg_hi, d_pub_counts, d_packbits, d_flag);
         ck(cudaGetLastError());
     }
