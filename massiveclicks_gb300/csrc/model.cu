@@ -11,6 +11,7 @@
 //   tiles     TileDev [n_tiles]    work queue (whole queries or query chunks)
 //   split_*   FP64 bins and counters of queries split over several tiles
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cstdint>
 #include <cstdio>
@@ -95,26 +96,45 @@ __global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32
         const unsigned word = __ballot_sync(0xffffffffu, m != 0u);
         const int64_t w0 = s0 + (threadIdx.x & ~31);  // first session of this warp, a multiple of 32
         if ((threadIdx.x & 31) == 0 && w0 < n) packbits[w0 >> 5] = word;
-        if (valid) {
-            seg = seg_id[s];
-            int last = 9, slot[MC_R];
+        // The rank loop runs on every lane (invalid lanes hold p = -1) so that
+        // lanes with the same qd at a rank -- consecutive sessions of one
+        // query mostly -- add their occurrence and click counts with one
+        // 64-bit atomic ({occurrences, clicks} as the low and high word).
+        if (valid) seg = seg_id[s];
+        int last = 9, slot[MC_R];
 #pragma unroll
-            for (int r = 0; r < MC_R; r++) {
-                int p = pidx_sm[s * MC_R + r];
+        for (int r = 0; r < MC_R; r++) {
+            int p = -1;
+            if (valid) {
+                p = pidx_sm[s * MC_R + r];
                 if (p < 0 || (int64_t)p >= n_qd) { atomicOr(flag, 1); p = 0; }
                 planes[(int64_t)r * stride + s] = p;
-                bool c = (m >> r) & 1u;
-                atomicAdd(&cnt[p].x, 1u);
-                if (c) atomicAdd(&cnt[p].y, 1u);
                 lo = min(lo, p);
                 hi = max(hi, p + 1);
-                slot[r] = r * (r + 1) / 2 + last;
-                if (c) last = r;
-                if (model == 0 && c) atomicAdd(&sc[r], 1u);
             }
-            int lc = m ? 31 - __clz(m) : MC_R;
-            if (model == 2) atomicAdd(&sc[MC_CNT_DBN_BEFORE_LAST], (unsigned)lc);
-            if (model == 1) atomicAdd(&sc[MC_CNT_CCM_UNCLICKED_BEFORE_LAST], (unsigned)(lc - __popc(m & ((1u << lc) - 1u))));
+            const bool c = valid && ((m >> r) & 1u);
+            const unsigned peers = __match_any_sync(0xffffffffu, p);
+            const unsigned clicked = __ballot_sync(0xffffffffu, c) & peers;
+            if (valid && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
+                atomicAdd(reinterpret_cast<unsigned long long*>(cnt + p),
+                          (unsigned long long)__popc(peers) | ((unsigned long long)__popc(clicked) << 32));
+            slot[r] = r * (r + 1) / 2 + last;
+            if (c) last = r;
+            if (model == 0) {  // clicks per rank, summed over the warp
+                const unsigned nc = __popc(__ballot_sync(0xffffffffu, c));
+                if ((threadIdx.x & 31) == 0 && nc) atomicAdd(&sc[r], nc);
+            }
+        }
+        {  // per-session counts of the public constants, summed over the warp
+            const int lc = m ? 31 - __clz(m) : MC_R;
+            unsigned v = 0;
+            if (valid && model == 2) v = (unsigned)lc;
+            if (valid && model == 1) v = (unsigned)(lc - __popc(m & ((1u << lc) - 1u)));
+            v = __reduce_add_sync(0xffffffffu, v);
+            if ((threadIdx.x & 31) == 0 && v)
+                atomicAdd(&sc[model == 2 ? MC_CNT_DBN_BEFORE_LAST : MC_CNT_CCM_UNCLICKED_BEFORE_LAST], v);
+        }
+        if (valid) {
             if (model == 3) {
 #pragma unroll
                 for (int r = 0; r < MC_R; r++) {
@@ -374,100 +394,136 @@ int mc_model::build_tiles() {
         return c;
     };
     const int64_t max_sess = std::max<int64_t>(spt, kTileSessions);
+    const size_t n_seg = seg_lo.size();
+    // Segments are tiled in fixed chunks of 65536 on several host threads (a
+    // chunk boundary also ends a tile, wherever the threads run); the chunks'
+    // tile and split lists are then joined in order.
+    auto build_range = [&](size_t g0, size_t g1, std::vector<TileDev>& tiles, std::vector<SplitDev>& splits,
+                           int64_t& bin_off) {
+        TileDev cur{};
+        bool open = false;
+        auto close = [&]() {
+            if (open) tiles.push_back(cur);
+            open = false;
+        };
+        auto new_split = [&](int64_t lo, int64_t hi) {
+            SplitDev sp;
+            sp.qd_begin = lo;
+            sp.qd_count = (int)(hi - lo);
+            sp.n_tiles = 0;
+            sp.bin_offset = bin_off;
+            sp.local = (int)splits.size();
+            sp.pad_ = 0;
+            bin_off += (hi - lo) * ns;
+            splits.push_back(sp);
+            return (int)splits.size() - 1;
+        };
+        auto split_tile = [&](int sid, int64_t b, int64_t e, int pk) {
+            TileDev t{};
+            t.fit = 0;
+            t.split = sid;
+            t.s_begin = b;
+            t.s_count = (int)(e - b);
+            t.qd_begin = splits[(size_t)sid].qd_begin;
+            t.qd_count = splits[(size_t)sid].qd_count;
+            t.blk_off = 0;
+            t.s_packed = pk;
+            tiles.push_back(t);
+            splits[(size_t)sid].n_tiles++;
+        };
+        for (size_t g = g0; g < g1; g++) {
+            const int64_t sb = seg_begin[g], sc = seg_begin[g + 1] - sb;
+            const int64_t lo = seg_lo[g], hi = seg_hi[g];
+            if (hi - lo > wqd) {  // direct: every session read from global memory
+                close();
+                const int sid = new_split(lo, hi);
+                const int64_t nt = (sc + spt - 1) / spt;
+                for (int64_t k = 0; k < nt; k++) {
+                    const int64_t b = sb + sc * k / nt, e = sb + sc * (k + 1) / nt;
+                    split_tile(sid, b, e, (int)(e - b));
+                }
+                continue;
+            }
+            const int64_t pk = packed_in(sb, sb + sc);
+            if (pk > spt || sc > max_sess) {  // staged split query
+                close();
+                const int sid = new_split(lo, hi);
+                const int64_t nt0 = std::max<int64_t>(1, (pk + spt - 1) / spt);
+                const int64_t target = std::max<int64_t>(1, (pk + nt0 - 1) / nt0);
+                const int64_t e = sb + sc;
+                int64_t b = sb;
+                int tpk = 0;
+                for (int64_t s = sb; s < e;) {
+                    // A whole aligned word that reaches neither bound is taken at once.
+                    if ((s & 31) == 0 && s + 32 <= e) {
+                        const int w = drop ? __builtin_popcount(packbits[(size_t)(s >> 5)]) : 32;
+                        if (tpk + w < target && s + 32 - b < max_sess) {
+                            tpk += w;
+                            s += 32;
+                            continue;
+                        }
+                    }
+                    tpk += packed_at(s);
+                    if ((tpk == target || s + 1 - b == max_sess) && s + 1 < e) {
+                        split_tile(sid, b, s + 1, tpk);
+                        b = s + 1;
+                        tpk = 0;
+                    }
+                    s++;
+                }
+                split_tile(sid, b, e, tpk);
+                continue;
+            }
+            if (open && (cur.s_packed + pk > spt || cur.s_count + sc > max_sess || hi - cur.qd_begin > wqd)) close();
+            if (!open) {
+                cur = TileDev{};
+                cur.fit = 0;
+                cur.split = -1;
+                cur.s_begin = sb;
+                cur.s_count = 0;
+                cur.s_packed = 0;
+                cur.qd_begin = lo;
+                open = true;
+            }
+            cur.s_count += (int)sc;
+            cur.s_packed += (int)pk;
+            cur.qd_count = (int)(hi - cur.qd_begin);
+        }
+        close();
+    };
+    const size_t kChunk = 65536;
+    const size_t n_chunks = (n_seg + kChunk - 1) / kChunk;
+    std::vector<std::vector<TileDev>> chunk_tiles(n_chunks);
+    std::vector<std::vector<SplitDev>> chunk_splits(n_chunks);
+    std::vector<int64_t> chunk_bins(n_chunks, 0);
+    {
+        std::atomic<size_t> next{0};
+        auto worker = [&]() {
+            for (size_t c; (c = next.fetch_add(1)) < n_chunks;)
+                build_range(c * kChunk, std::min(n_seg, (c + 1) * kChunk), chunk_tiles[c], chunk_splits[c], chunk_bins[c]);
+        };
+        const size_t nth = std::max<size_t>(1, std::min<size_t>(std::thread::hardware_concurrency(), n_chunks));
+        std::vector<std::thread> pool;
+        for (size_t t = 1; t < nth; t++) pool.emplace_back(worker);
+        worker();
+        for (auto& th : pool) th.join();
+    }
     std::vector<TileDev> tiles;
     std::vector<SplitDev> splits;
     int64_t bin_off = 0;
-    size_t n_seg = seg_lo.size();
-    TileDev cur{};
-    bool open = false;
-    auto close = [&]() {
-        if (open) tiles.push_back(cur);
-        open = false;
-    };
-    auto new_split = [&](int64_t lo, int64_t hi) {
-        SplitDev sp;
-        sp.qd_begin = lo;
-        sp.qd_count = (int)(hi - lo);
-        sp.n_tiles = 0;
-        sp.bin_offset = bin_off;
-        sp.local = (int)splits.size();
-        sp.pad_ = 0;
-        bin_off += (hi - lo) * ns;
-        splits.push_back(sp);
-        return (int)splits.size() - 1;
-    };
-    auto split_tile = [&](int sid, int64_t b, int64_t e, int pk) {
-        TileDev t{};
-        t.fit = 0;
-        t.split = sid;
-        t.s_begin = b;
-        t.s_count = (int)(e - b);
-        t.qd_begin = splits[(size_t)sid].qd_begin;
-        t.qd_count = splits[(size_t)sid].qd_count;
-        t.blk_off = 0;
-        t.s_packed = pk;
-        tiles.push_back(t);
-        splits[(size_t)sid].n_tiles++;
-    };
-    for (size_t g = 0; g < n_seg; g++) {
-        const int64_t sb = seg_begin[g], sc = seg_begin[g + 1] - sb;
-        const int64_t lo = seg_lo[g], hi = seg_hi[g];
-        if (hi - lo > wqd) {  // direct: every session read from global memory
-            close();
-            const int sid = new_split(lo, hi);
-            const int64_t nt = (sc + spt - 1) / spt;
-            for (int64_t k = 0; k < nt; k++) {
-                const int64_t b = sb + sc * k / nt, e = sb + sc * (k + 1) / nt;
-                split_tile(sid, b, e, (int)(e - b));
-            }
-            continue;
+    for (size_t c = 0; c < n_chunks; c++) {
+        const int soff = (int)splits.size();
+        for (TileDev t : chunk_tiles[c]) {
+            if (t.split >= 0) t.split += soff;
+            tiles.push_back(t);
         }
-        const int64_t pk = packed_in(sb, sb + sc);
-        if (pk > spt || sc > max_sess) {  // staged split query
-            close();
-            const int sid = new_split(lo, hi);
-            const int64_t nt0 = std::max<int64_t>(1, (pk + spt - 1) / spt);
-            const int64_t target = std::max<int64_t>(1, (pk + nt0 - 1) / nt0);
-            const int64_t e = sb + sc;
-            int64_t b = sb;
-            int tpk = 0;
-            for (int64_t s = sb; s < e;) {
-                // A whole aligned word that reaches neither bound is taken at once.
-                if ((s & 31) == 0 && s + 32 <= e) {
-                    const int w = drop ? __builtin_popcount(packbits[(size_t)(s >> 5)]) : 32;
-                    if (tpk + w < target && s + 32 - b < max_sess) {
-                        tpk += w;
-                        s += 32;
-                        continue;
-                    }
-                }
-                tpk += packed_at(s);
-                if ((tpk == target || s + 1 - b == max_sess) && s + 1 < e) {
-                    split_tile(sid, b, s + 1, tpk);
-                    b = s + 1;
-                    tpk = 0;
-                }
-                s++;
-            }
-            split_tile(sid, b, e, tpk);
-            continue;
+        for (SplitDev sp : chunk_splits[c]) {
+            sp.local += soff;
+            sp.bin_offset += bin_off;
+            splits.push_back(sp);
         }
-        if (open && (cur.s_packed + pk > spt || cur.s_count + sc > max_sess || hi - cur.qd_begin > wqd)) close();
-        if (!open) {
-            cur = TileDev{};
-            cur.fit = 0;
-            cur.split = -1;
-            cur.s_begin = sb;
-            cur.s_count = 0;
-            cur.s_packed = 0;
-            cur.qd_begin = lo;
-            open = true;
-        }
-        cur.s_count += (int)sc;
-        cur.s_packed += (int)pk;
-        cur.qd_count = (int)(hi - cur.qd_begin);
+        bin_off += chunk_bins[c];
     }
-    close();
     // Packed session blocks of the staged (non-direct) tiles, 16-byte aligned.
     // Sized by the packed counts, which the packing kernel checks.
     int64_t blk = 0;
