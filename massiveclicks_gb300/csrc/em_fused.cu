@@ -583,12 +583,26 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
         bulk_g2s(sb + L.atr_off, f.atr + a0, wn * 4, &full_bar[st]);
         if (f_sat) bulk_g2s(sb + L.sat_off, f_sat + a0, wn * 4, &full_bar[st]);
     };
+    // Tile indices come in runs of consecutive tiles (guided self-scheduling:
+    // a run is about 1/4 of the queue left per CTA, at most 16 and at least 1,
+    // estimated from the position this CTA last took), so a CTA's tiles are
+    // mostly neighbours: one fit, adjacent qd ranges.
+    int run_next = 0, run_end = 0;  // thread 0: the current run [run_next, run_end)
+    auto take_tile = [&]() -> int {
+        if (run_next >= run_end) {
+            int r = (n_tiles - run_end) / (4 * (int)gridDim.x);
+            r = r < 1 ? 1 : (r > 16 ? 16 : r);
+            run_next = (int)atomicAdd(&ws->next_tile, (unsigned)r);
+            run_end = run_next + r;
+        }
+        return run_next++;
+    };
     int t_pre = 0;   // thread 0: the next tile index, fetched an iteration ahead
     int filled = 0;  // thread 0: stage fills issued so far
     if (tid == 0) {
-        for (int s = 0; s < n_stages; s++) fill_stage(s, (int)atomicAdd(&ws->next_tile, 1u));
+        for (int s = 0; s < n_stages; s++) fill_stage(s, take_tile());
         filled = n_stages;
-        t_pre = (int)atomicAdd(&ws->next_tile, 1u);
+        t_pre = take_tile();
     }
 
     {
@@ -665,7 +679,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             if (ctid == 0 && k > 0) {
                 fill_stage((k - 1) % n_stages, t_pre);  // the (k - 1 + n_stages)-th tile
                 filled++;
-                t_pre = (int)atomicAdd(&ws->next_tile, 1u);
+                t_pre = take_tile();
             }
             TileDev tile{};
             if (t >= 0) tile = s_desc[k & 1];
