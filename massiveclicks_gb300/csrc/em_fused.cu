@@ -268,6 +268,22 @@ __device__ __forceinline__ void estep_ubm(const Src& src, const Sink& sink, int 
 // r + 1 possible slots is summed over the lanes that chose it.
 __device__ __forceinline__ void reduce_ubm_public(const int (&key)[MC_R], const float (&var)[MC_R], float* pub_tile) {
     int lane = threadIdx.x & 31;
+    // Sessions of a tile are sorted by click mask and the slots depend only on
+    // the mask, so most warps hold one key per rank in every lane: one sum
+    // and one atomic per rank.
+    bool same = true;
+#pragma unroll
+    for (int r = 0; r < MC_R; r++) same = same && key[r] == __shfl_sync(FULL_MASK, key[r], 0);
+    if (__all_sync(FULL_MASK, same)) {
+#pragma unroll
+        for (int r = 0; r < MC_R; r++) {
+            if (key[r] >= 0) {  // uniform over the warp
+                float v = warp_sum(var[r]);
+                if (lane == 0) atomicAdd(pub_tile + 2 * key[r], v);
+            }
+        }
+        return;
+    }
 #pragma unroll
     for (int r = 0; r < MC_R; r++) {
 #pragma unroll
