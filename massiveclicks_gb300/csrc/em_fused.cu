@@ -271,9 +271,13 @@ __device__ __forceinline__ void reduce_ubm_public(const int (&key)[MC_R], const 
     // Sessions of a tile are sorted by click mask and the slots depend only on
     // the mask, so most warps hold one key per rank in every lane: one sum
     // and one atomic per rank.
+    // Every lane executes every shuffle (no short-circuit around it).
     bool same = true;
 #pragma unroll
-    for (int r = 0; r < MC_R; r++) same = same && key[r] == __shfl_sync(FULL_MASK, key[r], 0);
+    for (int r = 0; r < MC_R; r++) {
+        const int k0 = __shfl_sync(FULL_MASK, key[r], 0);
+        same &= key[r] == k0;
+    }
     if (__all_sync(FULL_MASK, same)) {
 #pragma unroll
         for (int r = 0; r < MC_R; r++) {
