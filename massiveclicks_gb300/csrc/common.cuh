@@ -19,8 +19,9 @@
 #define MC_UBM_SLOTS 55
 #define MC_MAX_PUB 128         // >= 2 * public parameters of any model (UBM: 55 slots)
 
-// Fused kernel: at most this many threads per CTA (one producer warp plus the
-// consumer warps) and this many shared-memory stages in its copy ring.
+// Fused kernel: at most this many threads per CTA (every warp takes work
+// items; thread 0 also fills the copy ring), CTAs per SM it is compiled for,
+// and at most this many shared-memory stages in its copy ring.
 #define FUSED_THREADS 256
 #define FUSED_MIN_CTAS 2
 #define FUSED_MAX_STAGES 4

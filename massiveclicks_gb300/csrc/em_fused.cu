@@ -50,8 +50,9 @@
 //     product is the r-th prefix of one forward recursion P' = P - a E,
 //     E' = E g (1 - a) (E = P * examination), computed once per session;
 //   * the conditional examination at ranks >= l comes from the same unnormalised
-//     recursion restarted at each click, with a power-of-two rescale when P gets
-//     small (per-rank scaling), so no division is needed until the final ratio.
+//     recursion started at the last click (nothing before it feeds it), with a
+//     power-of-two rescale when P gets small (per-rank scaling), so no division
+//     is needed until the final ratio.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -125,7 +126,7 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                  : "memory");
 }
 __device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void consumer_sync(int n_threads) {
+__device__ __forceinline__ void workers_sync(int n_threads) {
     asm volatile("bar.sync 1, %0;" ::"r"(n_threads) : "memory");
 }
 
@@ -481,10 +482,10 @@ __device__ __forceinline__ void mstep_qd_d(int model, int mode, uint2 cnt, doubl
     }
 }
 
-// Public M-step of a fit whose last tile has finished (consumer threads of one CTA).
+// Public M-step of a fit whose last tile has finished (all threads of one CTA).
 __device__ void finalize_public(const FitDev& f, int ctid, int nc, int* s_it) {
     if (ctid == 0) *s_it = *(volatile int*)f.iter;
-    consumer_sync(nc);
+    workers_sync(nc);
     int nb = (*s_it + 1) & 1;
     for (int k = ctid; k < f.n_pub; k += nc) {
         double num = f.pub_const[2 * k] + ld_cg(f.pub_bins + 2 * k);
@@ -494,7 +495,7 @@ __device__ void finalize_public(const FitDev& f, int ctid, int nc, int* s_it) {
         f.pub_bins[2 * k] = 0.0;
         f.pub_bins[2 * k + 1] = 0.0;
     }
-    consumer_sync(nc);
+    workers_sync(nc);
     if (ctid == 0) {
         *f.tiles_done = 0;
         __threadfence();
@@ -650,24 +651,24 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             }
         };
         auto flush_fit = [&](const FitDev& f, unsigned count) {
-            consumer_sync(nc);
+            workers_sync(nc);
             for (int k = ctid; k < 2 * f.n_pub; k += nc) {
                 double v = pub_acc[k];
                 if (v != 0.0) atomicAdd(f.pub_bins + k, v);
                 pub_acc[k] = 0.0;
             }
             __threadfence();
-            consumer_sync(nc);
+            workers_sync(nc);
             if (ctid == 0) {
                 unsigned old = atomicAdd(f.tiles_done, count);
                 s_last = (old + count == (unsigned)f.n_tiles);
             }
-            consumer_sync(nc);
+            workers_sync(nc);
             if (s_last) {
                 __threadfence();
                 finalize_public(f, ctid, nc, &s_it);
             }
-            consumer_sync(nc);
+            workers_sync(nc);
         };
         auto next_chunk = [&]() {
             int c = 0;
@@ -678,13 +679,13 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
         for (int k = 0;; k++) {
             const int st = k % n_stages;
             const uint32_t round = (uint32_t)(k / n_stages);
-            // Every consumer thread observes the completed phase itself.
+            // Every thread observes the completed phase itself.
             if (!mbar_wait(&full_bar[st], round & 1u, status)) s_abort = 1;
             if (ctid == 0) {
                 s_chunk = 0;
                 s_desc[k & 1] = stage_desc[st];  // slot k & 1 last held tile k - 2, done
             }
-            consumer_sync(nc);
+            workers_sync(nc);
             if (*(volatile int*)&s_abort) {
                 // Copies this CTA issued may still be in flight: the previous
                 // tile's counts and the stages filled but not yet consumed.
@@ -723,7 +724,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
                 const FitDev& fg = fits[cur_fit];
                 int it = *(volatile int*)fg.iter;
                 for (int q = ctid; q < fg.n_pub; q += nc) pub_th[q] = fg.pub_theta[(it & 1) * MC_MAX_PUB + q];
-                consumer_sync(nc);
+                workers_sync(nc);
             }
             if (warp == 0 && !folded) fold_pub((k - 1) & 1, s_fit[pfs]);
             // Click counts of this tile's window for its M-step (next
@@ -896,7 +897,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             // A direct tile's statistics went to global memory: order them
             // before the barrier, after which the split counter is raised.
             if (direct) __threadfence();
-            consumer_sync(nc);
+            workers_sync(nc);
             if (t < 0) break;
             prev_t = t;
             pfs = fs;
