@@ -323,8 +323,12 @@ __device__ __forceinline__ void estep_dbn(const Src& src, const Sink& sink, int 
     // Only a, car and the all-unclicked prefix products stay in registers;
     // satisfaction values and window indices are re-read from shared memory.
     float a[MC_R];
+    int rls[MC_R];
 #pragma unroll
-    for (int r = 0; r < MC_R; r++) a[r] = src.a(src.rel_at(r, sl));
+    for (int r = 0; r < MC_R; r++) {
+        rls[r] = src.rel_at(r, sl);
+        a[r] = src.a(rls[r]);
+    }
     // car_r = a_r + g (1 - a_r) car_{r+1}, car_10 = 0 (compute_exm_car).
     float car[MC_R + 1];
     car[MC_R] = 0.0f;
@@ -349,7 +353,7 @@ __device__ __forceinline__ void estep_dbn(const Src& src, const Sink& sink, int 
     float eps = 1.0f, P = 1.0f, E = 1.0f;
 #pragma unroll
     for (int r = 0; r < MC_R; r++) {
-        const int rl = src.rel_at(r, sl);
+        const int rl = rls[r];
         const float s_r = src.s(rl);
         const float R = (r < MC_R - 1) ? Pu[MC_R - 1 - r] : 1.0f;
         if (r < l) {
@@ -389,8 +393,12 @@ __device__ __forceinline__ void estep_ccm(const Src& src, const Sink& sink, int 
     const int l = m ? 31 - __clz(m) : MC_R;
     if (l == MC_R) return;  // constant contributions only (added at upload)
     float a[MC_R];
+    int rls[MC_R];
 #pragma unroll
-    for (int r = 0; r < MC_R; r++) a[r] = src.a(src.rel_at(r, sl));
+    for (int r = 0; r < MC_R; r++) {
+        rls[r] = src.rel_at(r, sl);
+        a[r] = src.a(rls[r]);
+    }
     float car[MC_R + 1];
     car[MC_R] = 0.0f;
 #pragma unroll
@@ -431,14 +439,14 @@ __device__ __forceinline__ void estep_ccm(const Src& src, const Sink& sink, int 
             t[2] += ia * t2 * R * B; t[3] += ia * k2 * B;
             t[4] += a[r] * t3 * R * B; t[5] += a[r] * k3 * B;
             float cont = t2 * ia + t3 * a[r];
-            sink.add(src.rel_at(r, sl), 0, __fdividef(a[r], 1.0f - cont * car[r + 1]));
+            sink.add(rls[r], 0, __fdividef(a[r], 1.0f - cont * car[r + 1]));
             E = cont;
             P = 1.0f;
         } else {
             float D = __fdividef(1.0f, P - t1 * E * (1.0f - R));
             t[0] += t1 * R * E * D;
             t[1] += E * (1.0f - t1 * (1.0f - R)) * D;
-            sink.add(src.rel_at(r, sl), 0, __fdividef((1.0f - eps) * a[r], 1.0f - eps * car[r]));
+            sink.add(rls[r], 0, __fdividef((1.0f - eps) * a[r], 1.0f - eps * car[r]));
             P = P - a[r] * E;
             E = E * t1 * ia;
             rescale(P, E);
