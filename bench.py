@@ -214,7 +214,10 @@ def run_reference(args, rank: int, world: int):
         return
     threads = os.cpu_count() or 1
     ds, prep = make_dataset(args, 0)
-    n = cpu_sample(ds, args.cpu_sample)
+    # The per-step sample shrinks with --steps so that the arm stays near a
+    # minute of CPU work (at most 250M session-iterations, at least 50,000
+    # sessions per step).
+    n = cpu_sample(ds, min(args.cpu_sample, max(50_000, 250_000_000 // max(1, args.steps))))
     times = time_cpu_oracle(ds, n, args.steps, max(1, min(args.warmup, 2)), threads)
     total = sum(times)
     value = n * len(times) / total
