@@ -546,6 +546,9 @@ __host__ __device__ inline Layout make_layout(int model, int spt, int window_max
 template <int MODEL>
 __device__ __forceinline__ int model_of(const FitDev& f) { return MODEL >= 0 ? MODEL : f.model; }
 
+// qd per lane in one owned-tile M-step item (an item covers 32 * kMQ qd).
+constexpr int kMQ = 4;
+
 template <int MODEL>
 __global__ void __launch_bounds__(FUSED_THREADS, FUSED_MIN_CTAS)
 em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ tiles, int n_tiles,
@@ -755,7 +758,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             const bool direct = t >= 0 && tile.qd_count > window_max;
             const int n_sess = t < 0 ? 0 : (direct ? tile.s_count : tile.s_packed);
             const int nE = (n_sess + 31) >> 5;
-            const int nM = prev_t < 0 ? 0 : (ptile.split >= 0 ? 1 : (ptile.qd_count + 63) >> 6);
+            const int nM = prev_t < 0 ? 0 : (ptile.split >= 0 ? 1 : (ptile.qd_count + 32 * kMQ - 1) / (32 * kMQ));
             if (prev_t >= 0 && ptile.split < 0 &&
                 !mbar_wait(&cnt_bar[(k - 1) & 1], ((uint32_t)(k - 1) >> 1) & 1u, status))
                 s_abort = 1;  // counts unreliable; the status word already says so
@@ -765,7 +768,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             float* bins_m = bins + ((k - 1) & 1) * L.bins_buf;
             float* pub_k = pub_tile[k & 1];
 
-            // M-step items of the previous tile.  Owned tile: 64 qd per item,
+            // M-step items of the previous tile.  Owned tile: 32 * kMQ qd per item,
             // straight from the bins and the counts, written in place.  Split
             // tile: one item, the warp folds the bins into the query's FP64
             // bins and, if its tile is the query's last, runs the query's M-step.
@@ -774,23 +777,24 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
                 const int pmodel = model_of<MODEL>(pf);
                 const int pns = private_stats(pmodel);
                 if (ptile.split < 0) {
-                    const int i0 = (mi << 6) + lane, i1 = i0 + 32;
-                    const bool h0 = i0 < ptile.qd_count, h1 = i1 < ptile.qd_count;
-                    const uint32_t p0 = h0 ? cnt_m[i0] : 0u, p1 = h1 ? cnt_m[i1] : 0u;
-                    const uint2 c0 = make_uint2(p0 & 0xFFFFu, p0 >> 16), c1 = make_uint2(p1 & 0xFFFFu, p1 >> 16);
-                    if (h0) {
-                        float v0 = bins_m[i0], v1 = 0.0f;
-                        bins_m[i0] = 0.0f;
-                        if (pns > 1) { v1 = bins_m[L.bins_stride + i0]; bins_m[L.bins_stride + i0] = 0.0f; }
-                        const int64_t q = ptile.qd_begin + i0;
-                        mstep_qd_f(pmodel, pf.mode, c0, v0, v1, pf.atr + q, pns > 1 ? pf.sat + q : nullptr);
+                    // kMQ qd per lane; the counts are loaded first, then each qd's update.
+                    uint32_t pc[kMQ];
+#pragma unroll
+                    for (int j = 0; j < kMQ; j++) {
+                        const int i = mi * (32 * kMQ) + j * 32 + lane;
+                        pc[j] = i < ptile.qd_count ? cnt_m[i] : 0u;
                     }
-                    if (h1) {
-                        float v0 = bins_m[i1], v1 = 0.0f;
-                        bins_m[i1] = 0.0f;
-                        if (pns > 1) { v1 = bins_m[L.bins_stride + i1]; bins_m[L.bins_stride + i1] = 0.0f; }
-                        const int64_t q = ptile.qd_begin + i1;
-                        mstep_qd_f(pmodel, pf.mode, c1, v0, v1, pf.atr + q, pns > 1 ? pf.sat + q : nullptr);
+#pragma unroll
+                    for (int j = 0; j < kMQ; j++) {
+                        const int i = mi * (32 * kMQ) + j * 32 + lane;
+                        if (i < ptile.qd_count) {
+                            float v0 = bins_m[i], v1 = 0.0f;
+                            bins_m[i] = 0.0f;
+                            if (pns > 1) { v1 = bins_m[L.bins_stride + i]; bins_m[L.bins_stride + i] = 0.0f; }
+                            const int64_t q = ptile.qd_begin + i;
+                            mstep_qd_f(pmodel, pf.mode, make_uint2(pc[j] & 0xFFFFu, pc[j] >> 16), v0, v1, pf.atr + q,
+                                       pns > 1 ? pf.sat + q : nullptr);
+                        }
                     }
                     return;
                 }
