@@ -377,7 +377,7 @@ __device__ __forceinline__ void estep_dbn(const Src& src, const Sink& sink, int 
             E = E * g * (1.0f - a[r]);
             rescale(P, E);
         }
-        eps *= g * (1.0f - a[r]) + g * a[r] * (1.0f - s_r);
+        eps *= g * (1.0f - a[r] * s_r);  // g (1 - a) + g a (1 - s)
     }
 }
 
