@@ -368,13 +368,15 @@ __device__ __forceinline__ void estep_dbn(const Src& src, const Sink& sink, int 
             E = g * cs;
             P = 1.0f;
         } else {
-            // Unclicked rank after the last click.
-            float D = __fdividef(1.0f, P - g * E * (1.0f - R));
-            gnum += g * R * E * D;
-            gden += E * (1.0f - g * (1.0f - R)) * D;
+            // Unclicked rank after the last click (t = g E, u = t (1 - R)).
+            const float t = g * E;
+            const float u = t * (1.0f - R);
+            const float D = __fdividef(1.0f, P - u);
+            gnum += t * R * D;
+            gden += (E - u) * D;
             sink.add(rl, 0, __fdividef(a[r] * (1.0f - eps), 1.0f - eps * car[r]));
             P = P - a[r] * E;
-            E = E * g * (1.0f - a[r]);
+            E = t * (1.0f - a[r]);
             rescale(P, E);
         }
         eps *= g * (1.0f - a[r] * s_r);  // g (1 - a) + g a (1 - s)
