@@ -116,22 +116,37 @@ def make_dataset(args, rank: int):
     return ds, {"generate_s": round(t1 - t0, 3), "ingest_s": round(t2 - t1, 3)}
 
 
-def cpu_sample(ds, n_sample: int):
-    """A query-aligned prefix of the sorted training set."""
-    n = min(n_sample, len(ds.train))
+def cpu_sample(ds, n_sample: int) -> np.ndarray:
+    """Indices of a bounded sample of the sorted training set: whole queries,
+    visited in a seeded random order (so head and tail queries both appear)
+    and taken while they fit in what is left of the budget, then put back in
+    sorted order."""
     q = ds.train.query
-    while 0 < n < len(q) and q[n] == q[n - 1]:
-        n += 1
-    return n
+    if len(q) == 0:
+        return np.zeros(0, np.int64)
+    starts = np.flatnonzero(np.r_[True, q[1:] != q[:-1]])
+    ends = np.r_[starts[1:], len(q)]
+    chosen, left = [], n_sample
+    for g in np.random.default_rng(0).permutation(len(starts)).tolist():
+        size = int(ends[g] - starts[g])
+        if size <= left:
+            chosen.append(g)
+            left -= size
+            if left == 0:
+                break
+    chosen.sort()
+    return np.concatenate([np.arange(starts[g], ends[g]) for g in chosen]) if chosen else np.zeros(0, np.int64)
 
 
-def time_cpu_oracle(ds, n: int, iters: int, warmup: int, threads: int):
+def time_cpu_oracle(ds, idx: np.ndarray, iters: int, warmup: int, threads: int):
     """The reference's CPU path (FP32 restatement, reference threading) on the
-    first n training sessions: seconds per iteration, one entry per step."""
+    training sessions idx (whole queries): seconds per iteration, one entry
+    per step."""
     from oracle import bindings
     sub = ds.train
-    nq = int(sub.pidx[:n].max()) + 1 if n else 0
-    fit = bindings.OracleFit("f32", 2, 0, sub.query[:n], sub.pidx[:n], sub.click[:n], nq)
+    p = sub.pidx[idx]
+    nq = int(p.max()) + 1 if len(idx) else 0
+    fit = bindings.OracleFit("f32", 2, 0, sub.query[idx], p, sub.click[idx], nq)
     fit.run(warmup, threads)
     times = []
     for _ in range(iters):
@@ -217,8 +232,9 @@ def run_reference(args, rank: int, world: int):
     # The per-step sample shrinks with --steps so that the arm stays near a
     # minute of CPU work (at most 250M session-iterations, at least 50,000
     # sessions per step).
-    n = cpu_sample(ds, min(args.cpu_sample, max(50_000, 250_000_000 // max(1, args.steps))))
-    times = time_cpu_oracle(ds, n, args.steps, max(1, min(args.warmup, 2)), threads)
+    idx = cpu_sample(ds, min(args.cpu_sample, max(50_000, 250_000_000 // max(1, args.steps))))
+    n = len(idx)
+    times = time_cpu_oracle(ds, idx, args.steps, max(1, min(args.warmup, 2)), threads)
     total = sum(times)
     value = n * len(times) / total
     line = {
@@ -230,7 +246,7 @@ def run_reference(args, rank: int, world: int):
                    "sessions": args.sessions, "train_sessions": len(ds.train), "sample_sessions": n,
                    "parallelism": f"{threads} host threads"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"first {n} training sessions (query-aligned) of the 16M, {len(times)} iterations"},
+                         "sample": f"{n} training sessions (whole queries) of the 16M, {len(times)} iterations"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -387,10 +403,11 @@ def run_ours(args, rank: int, world: int, local: int):
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        n = cpu_sample(ds, args.cpu_sample)
-        times = time_cpu_oracle(ds, n, 2, 1, threads)
+        idx = cpu_sample(ds, args.cpu_sample)
+        n = len(idx)
+        times = time_cpu_oracle(ds, idx, 2, 1, threads)
         cpu = {"value": n * len(times) / sum(times), "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"first {n} training sessions (query-aligned), {len(times)} iterations after 1 warm-up; "
+               "sample": f"{n} training sessions (whole queries), {len(times)} iterations after 1 warm-up; "
                          "FP32 restatement of the reference's CPU path with its threading"}
 
     if rank == 0:
