@@ -195,6 +195,16 @@ int mc_model_set_param(mc_model* m, int index, const float* values, void* stream
 int mc_model_evaluate(mc_model* m, int which, double* ll_sum, double* log2_sums, int64_t* n_sessions,
                       void* stream);
 
+/* Training log-likelihood per iteration: n_iterations fused iterations, each
+ * followed on the device by the evaluation of the training sessions under the
+ * parameters that iteration produced; train_ll[i] (host, n_iterations values)
+ * receives ll_sum of mc_model_evaluate(which = 0) after iteration i + 1.  The
+ * reference logs only the final test-set values (parallel_em.cu:634-723);
+ * this traces convergence without a host round trip between iterations.
+ * Allocates a device array of 88 * n_iterations bytes for the call.
+ * Synchronous. */
+int mc_model_em_trace(mc_model* m, int32_t n_iterations, double* train_ll, void* stream);
+
 /* Device memory held by the model, in bytes. */
 int mc_model_memory(const mc_model* m, int64_t* bytes);
 

@@ -208,6 +208,13 @@ class ClickModel:
     def em(self, iterations: int, impl: int = IMPL_FUSED, stream=None) -> None:
         check(_capi.load().mc_model_em(self._h, int(iterations), int(impl), _stream(stream)))
 
+    def em_trace(self, iterations: int, stream=None) -> np.ndarray:
+        """Fused iterations with the training log-likelihood (per session, as
+        evaluate(0).llh) after each one, computed on the device."""
+        out = np.zeros(max(int(iterations), 0), np.float64)  # a negative count is the library's to reject
+        check(_capi.load().mc_model_em_trace(self._h, int(iterations), _ptr(out), _stream(stream)))
+        return out / max(self.n_train, 1)
+
     def process_session(self, stream=None) -> None:
         check(_capi.load().mc_model_process_sessions(self._h, _stream(stream)))
 

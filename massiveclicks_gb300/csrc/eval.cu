@@ -24,7 +24,7 @@ __global__ void __launch_bounds__(256) eval_kernel(EvalArgs A) {
     double acc[MC_R + 1];
 #pragma unroll
     for (int k = 0; k <= MC_R; k++) acc[k] = 0.0;
-    const float* pub = A.pub;
+    const float* pub = A.iter ? A.pub + (*A.iter & 1) * MC_MAX_PUB : A.pub;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < A.n; s += stride) {
         unsigned m = A.click[s];

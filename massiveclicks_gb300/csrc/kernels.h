@@ -56,6 +56,9 @@ struct EvalArgs {
     const float* sat;
     const float* pub;       // current public values
     double* out;            // [11]: log-likelihood sum, then log2 sums per rank
+    // Optional: with iter set, pub is the [2][MC_MAX_PUB] double buffer and
+    // the half (*iter & 1) read on the device is the current one.
+    const int* iter = nullptr;
 };
 
 cudaError_t launch_eval(const EvalArgs& A, int n_sm, cudaStream_t st);

@@ -1110,6 +1110,53 @@ extern "C" int mc_model_evaluate(mc_model* m, int which, double* ll_sum, double*
     return MC_OK;
 }
 
+extern "C" int mc_model_em_trace(mc_model* m, int32_t iters, double* train_ll, void* stream) {
+    if (!m) return set_error(MC_ERR_INVALID, "em_trace: null model");
+    if (!m->uploaded) return set_error(MC_ERR_STATE, "em_trace: no training sessions uploaded");
+    if (iters < 0) return set_error(MC_ERR_INVALID, "em_trace: negative iteration count");
+    if (iters > 0 && !train_ll) return set_error(MC_ERR_INVALID, "em_trace: null output");
+    if (!m->fused_ok) return set_error(MC_ERR_INVALID, "em_trace: fused path unavailable: " + m->fused_reason);
+    CK(cudaSetDevice(m->device));
+    cudaStream_t st = m->pick(stream);
+    if (iters == 0) return MC_OK;
+    if (m->n == 0) {
+        for (int i = 0; i < iters; i++) train_ll[i] = 0.0;
+        return MC_OK;
+    }
+    double* d_trace = nullptr;
+    int64_t scratch = 0;
+    int rc = dalloc(&d_trace, (size_t)iters * (MC_R + 1), &scratch);
+    if (rc) return rc;
+    std::vector<double> host((size_t)iters * (MC_R + 1));
+    cudaError_t e = cudaSuccess;
+    auto ck = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+    ck(cudaMemsetAsync(d_trace, 0, host.size() * 8, st));
+    EvalArgs A;
+    A.model = m->model;
+    A.n = m->n;
+    A.stride = m->stride;
+    A.n_qd = m->n_qd;
+    A.pidx = m->d_pidx;
+    A.click = m->d_click;
+    A.atr = m->d_atr;
+    A.sat = m->d_sat;
+    A.pub = m->d_pub_theta;
+    A.iter = m->d_iter;  // the public half written by the iteration just run
+    for (int i = 0; i < iters && e == cudaSuccess; i++) {
+        ck(launch_em_fused(m->model, m->d_fit, m->d_tiles, m->n_tiles, m->d_splits, m->d_ws, m->wqd, m->spt,
+                           m->stages, m->grid, m->block, st));
+        A.out = d_trace + (int64_t)i * (MC_R + 1);
+        ck(launch_eval(A, m->n_sm, st));
+    }
+    ck(cudaMemcpyAsync(host.data(), d_trace, host.size() * 8, cudaMemcpyDeviceToHost, st));
+    ck(cudaStreamSynchronize(st));
+    dfree(d_trace);
+    if (e != cudaSuccess) return cuda_fail("em_trace", e);
+    if ((rc = check_status(m, st))) return rc;
+    for (int i = 0; i < iters; i++) train_ll[i] = host[(size_t)i * (MC_R + 1)];
+    return MC_OK;
+}
+
 extern "C" int mc_model_autotune(mc_model* m, void* stream) {
     if (!m) return set_error(MC_ERR_INVALID, "autotune: null model");
     if (!m->uploaded || !m->fused_ok) return set_error(MC_ERR_STATE, "autotune: needs uploaded sessions and the fused path");
