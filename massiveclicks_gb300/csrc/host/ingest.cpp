@@ -82,10 +82,17 @@ static void build_partition(const std::vector<int32_t>& query, const std::vector
     int64_t n_test = n - n_train;
 
     // Sort the training sessions by query with the reference's comparator.
+    // The elements are (query, index) pairs compared by query alone: std::sort
+    // then makes the same comparisons with the same outcomes and the same
+    // moves as on the sessions themselves, so it leaves the indices in the
+    // reference's (unstable) order, without a random load per comparison.
+    std::vector<std::pair<int32_t, int32_t>> kv((size_t)n_train);
+    for (int64_t i = 0; i < n_train; i++) kv[(size_t)i] = {query[(size_t)i], (int32_t)i};
+    std::sort(kv.begin(), kv.end(),
+              [](const std::pair<int32_t, int32_t>& a, const std::pair<int32_t, int32_t>& b) { return a.first < b.first; });
     std::vector<int32_t> order((size_t)n_train);
-    std::iota(order.begin(), order.end(), 0);
-    const int32_t* q = query.data();
-    std::sort(order.begin(), order.end(), [q](int32_t a, int32_t b) { return q[a] < q[b]; });
+    for (int64_t i = 0; i < n_train; i++) order[(size_t)i] = kv[(size_t)i].second;
+    std::vector<std::pair<int32_t, int32_t>>().swap(kv);
 
     SessionSet& tr = d->train;
     tr.query.resize((size_t)n_train);
@@ -110,23 +117,33 @@ static void build_partition(const std::vector<int32_t>& query, const std::vector
     // indices 0..k-1; the lookup table keeps (doc, local index) sorted by doc.
     std::vector<int64_t> seg_ndocs(n_seg, 0);
     std::vector<std::vector<std::pair<int32_t, int32_t>>> seg_lookup(n_seg);
-    auto index_segment = [&](size_t s) {
+    struct Scratch {
+        std::vector<uint64_t> keys;
+        std::vector<std::pair<uint32_t, uint32_t>> firsts;
+        std::vector<uint32_t> by_first;
+        std::vector<int32_t> local;
+    };
+    auto index_segment = [&](size_t s, Scratch& sc) {
         int64_t b = seg_begin[s], e = seg_begin[s + 1];
         size_t m = (size_t)(e - b) * MC_MAX_SERP;
-        std::vector<uint64_t> keys(m);
+        std::vector<uint64_t>& keys = sc.keys;
+        keys.resize(m);
         for (size_t k = 0; k < m; k++) {
             uint32_t doc = (uint32_t)tr.docs[(size_t)b * MC_MAX_SERP + k];
             keys[k] = ((uint64_t)(doc ^ 0x80000000u) << 32) | (uint64_t)k;  // signed doc order
         }
         std::sort(keys.begin(), keys.end());
         // Groups of equal doc: first element carries the first appearance.
-        std::vector<std::pair<uint32_t, uint32_t>> firsts;  // (first position, group start)
+        std::vector<std::pair<uint32_t, uint32_t>>& firsts = sc.firsts;  // (first position, group start)
+        firsts.clear();
         for (size_t k = 0; k < m; k++)
             if (k == 0 || (keys[k] >> 32) != (keys[k - 1] >> 32)) firsts.push_back({(uint32_t)(keys[k] & 0xffffffffu), (uint32_t)k});
-        std::vector<uint32_t> by_first(firsts.size());
+        std::vector<uint32_t>& by_first = sc.by_first;
+        by_first.resize(firsts.size());
         std::iota(by_first.begin(), by_first.end(), 0);
         std::sort(by_first.begin(), by_first.end(), [&](uint32_t x, uint32_t y) { return firsts[x].first < firsts[y].first; });
-        std::vector<int32_t> local(firsts.size());
+        std::vector<int32_t>& local = sc.local;
+        local.resize(firsts.size());
         for (size_t r = 0; r < by_first.size(); r++) local[by_first[r]] = (int32_t)r;
         auto& lk = seg_lookup[s];
         lk.resize(firsts.size());
@@ -144,7 +161,10 @@ static void build_partition(const std::vector<int32_t>& query, const std::vector
     {
         std::vector<std::thread> pool;
         for (size_t t = 0; t < n_threads; t++)
-            pool.emplace_back([&, t]() { for (size_t s = t; s < n_seg; s += n_threads) index_segment(s); });
+            pool.emplace_back([&, t]() {
+                Scratch sc;
+                for (size_t s = t; s < n_seg; s += n_threads) index_segment(s, sc);
+            });
         for (auto& th : pool) th.join();
     }
     std::vector<int64_t> seg_base(n_seg + 1, 0);
@@ -163,99 +183,204 @@ static void build_partition(const std::vector<int32_t>& query, const std::vector
     }
     d->n_qd = seg_base[n_seg];
 
-    // Test set: the tail in arrival order, filtered.
+    // Test set: the tail in arrival order, filtered; contiguous ranges on
+    // several threads, joined in order.
+    auto filter_range = [&](int64_t i0, int64_t i1, SessionSet& out) {
+        for (int64_t i = i0; i < i1; i++) {
+            int32_t qi = query[(size_t)i];
+            size_t lo = 0, hi = n_seg;
+            while (lo < hi) {  // first segment with query >= qi
+                size_t mid = (lo + hi) / 2;
+                if (tr.query[(size_t)seg_begin[mid]] < qi) lo = mid + 1; else hi = mid;
+            }
+            if (lo == n_seg || tr.query[(size_t)seg_begin[lo]] != qi) continue;
+            const auto& lk = seg_lookup[lo];
+            int32_t p[MC_MAX_SERP];
+            bool any = false;
+            for (int r = 0; r < MC_MAX_SERP; r++) {
+                int32_t doc = docs[(size_t)i * MC_MAX_SERP + r];
+                auto it = std::lower_bound(lk.begin(), lk.end(), std::make_pair(doc, INT_MIN));
+                if (it != lk.end() && it->first == doc) { p[r] = (int32_t)seg_base[lo] + it->second; any = true; }
+                else p[r] = -1;
+            }
+            if (!any) continue;
+            out.query.push_back(qi);
+            for (int r = 0; r < MC_MAX_SERP; r++) {
+                out.docs.push_back(docs[(size_t)i * MC_MAX_SERP + r]);
+                out.pidx.push_back(p[r]);
+            }
+            out.click.push_back(click[(size_t)i]);
+        }
+    };
+    const int64_t n_tparts = std::max<int64_t>(1, std::min<int64_t>(hw, n_test / 65536));
+    std::vector<SessionSet> tparts((size_t)n_tparts);
+    {
+        std::vector<std::thread> pool;
+        for (int64_t t = 0; t < n_tparts; t++)
+            pool.emplace_back([&, t]() {
+                filter_range(n_train + n_test * t / n_tparts, n_train + n_test * (t + 1) / n_tparts, tparts[(size_t)t]);
+            });
+        for (auto& th : pool) th.join();
+    }
     SessionSet& te = d->test;
-    for (int64_t i = n_train; i < n; i++) {
-        int32_t qi = query[(size_t)i];
-        size_t lo = 0, hi = n_seg;
-        while (lo < hi) {  // first segment with query >= qi
-            size_t mid = (lo + hi) / 2;
-            if (tr.query[(size_t)seg_begin[mid]] < qi) lo = mid + 1; else hi = mid;
-        }
-        if (lo == n_seg || tr.query[(size_t)seg_begin[lo]] != qi) continue;
-        const auto& lk = seg_lookup[lo];
-        int32_t p[MC_MAX_SERP];
-        bool any = false;
-        for (int r = 0; r < MC_MAX_SERP; r++) {
-            int32_t doc = docs[(size_t)i * MC_MAX_SERP + r];
-            auto it = std::lower_bound(lk.begin(), lk.end(), std::make_pair(doc, INT_MIN));
-            if (it != lk.end() && it->first == doc) { p[r] = (int32_t)seg_base[lo] + it->second; any = true; }
-            else p[r] = -1;
-        }
-        if (!any) continue;
-        te.query.push_back(qi);
-        for (int r = 0; r < MC_MAX_SERP; r++) {
-            te.docs.push_back(docs[(size_t)i * MC_MAX_SERP + r]);
-            te.pidx.push_back(p[r]);
-        }
-        te.click.push_back(click[(size_t)i]);
+    for (const SessionSet& part : tparts) {
+        te.query.insert(te.query.end(), part.query.begin(), part.query.end());
+        te.docs.insert(te.docs.end(), part.docs.begin(), part.docs.end());
+        te.pidx.insert(te.pidx.end(), part.pidx.begin(), part.pidx.end());
+        te.click.insert(te.click.end(), part.click.begin(), part.click.end());
     }
     (void)n_test;
 }
 
-static void tokenize(const std::string& line, std::vector<std::pair<const char*, const char*>>& tok) {
-    tok.clear();
-    const char* p = line.data();
-    const char* e = p + line.size();
+// One parsed line.  kind: 1 query line (15 tokens), 2 click line (4 tokens),
+// 3 other token count (reported, but its session id still becomes the last
+// one seen), 0 rejected (bad session id or field: reported, no state change).
+struct ParsedLine {
+    const char* b;  // the line's text, for the report
+    const char* e;
+    int32_t sid;
+    int32_t query;
+    int32_t v[MC_MAX_SERP];  // query line: docs; click line: v[0] = doc
+    uint8_t kind;
+};
+
+static inline bool is_space(char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r'; }
+
+// Tokens as the reference's std::istringstream >> splits them (whitespace).
+static ParsedLine parse_line(const char* b, const char* e) {
+    ParsedLine pl;
+    pl.b = b;
+    pl.e = e;
+    pl.kind = 0;
+    pl.sid = 0;
+    pl.query = 0;
+    const char* tb[16];
+    const char* te[16];
+    int nt = 0;
+    const char* p = b;
     while (p < e) {
-        while (p < e && std::isspace((unsigned char)*p)) p++;
+        while (p < e && is_space(*p)) p++;
         if (p >= e) break;
-        const char* s = p;
-        while (p < e && !std::isspace((unsigned char)*p)) p++;
-        tok.push_back({s, p});
+        const char* s0 = p;
+        while (p < e && !is_space(*p)) p++;
+        if (nt < 16) { tb[nt] = s0; te[nt] = p; }
+        nt++;
     }
+    if (nt == 0 || !parse_int(tb[0], te[0], &pl.sid)) return pl;
+    if (nt == 15) {
+        bool ok = parse_int(tb[3], te[3], &pl.query);
+        for (int r = 0; r < MC_MAX_SERP && ok; r++) ok = parse_int(tb[5 + r], te[5 + r], &pl.v[r]);
+        if (ok) pl.kind = 1;
+    } else if (nt == 4) {
+        if (parse_int(tb[3], te[3], &pl.v[0])) pl.kind = 2;
+    } else {
+        pl.kind = 3;
+    }
+    return pl;
 }
 
 }  // namespace mch
 
 using namespace mch;
 
+// The text log is read in blocks; the lines of a block are parsed by several
+// threads (each a contiguous run of lines) and then replayed in order through
+// the reference's session state machine (dataset.cpp:224-305): the session
+// count is checked before every line, a query line closes the open session
+// when a previous line set a session id other than -1, a click line marks the
+// first matching doc, and the open session at the stop is dropped.
 extern "C" int mc_dataset_parse(const char* path, int32_t max_sessions, float test_share, mc_dataset** out) {
     if (!path || !out) return set_error(MC_ERR_INVALID, "dataset_parse: null argument");
     *out = nullptr;
     if (!(test_share >= 0.0f && test_share <= 1.0f))
         return set_error(MC_ERR_INVALID, "dataset_parse: test_share must be in [0, 1]");
-    std::ifstream f(path);
-    if (!f.is_open()) return set_error(MC_ERR_IO, std::string("Unable to open the raw dataset: ") + path);
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return set_error(MC_ERR_IO, std::string("Unable to open the raw dataset: ") + path);
 
     std::vector<int32_t> query, docs;
     std::vector<uint16_t> click;
-    std::string line;
-    std::vector<std::pair<const char*, const char*>> tok;
     RawSession cur;
     int64_t n_queries = 0;
     long long session_prev = -1;
     bool have_prev = false;
-    while ((n_queries < max_sessions || max_sessions == -1) && std::getline(f, line)) {
-        tokenize(line, tok);
-        int32_t sid;
-        if (tok.empty() || !parse_int(tok[0].first, tok[0].second, &sid)) {
-            std::cout << "\nInvalid data: " << line << std::endl;
-            continue;
-        }
-        if (tok.size() == 15) {
-            RawSession next;
-            bool ok = parse_int(tok[3].first, tok[3].second, &next.query);
-            for (int r = 0; r < MC_MAX_SERP && ok; r++) ok = parse_int(tok[5 + r].first, tok[5 + r].second, &next.docs[r]);
-            if (!ok) { std::cout << "\nInvalid data: " << line << std::endl; continue; }
-            if (have_prev && session_prev != -1) {
-                query.push_back(cur.query);
-                docs.insert(docs.end(), cur.docs, cur.docs + MC_MAX_SERP);
-                click.push_back(cur.click);
-                n_queries++;
+    bool done = false;
+
+    const size_t kBlock = (size_t)64 << 20;
+    const unsigned n_threads = std::max(1u, std::thread::hardware_concurrency());
+    std::vector<char> buf;
+    std::string carry;  // the unfinished last line of the previous block
+    std::vector<std::vector<ParsedLine>> parts(n_threads);
+    bool eof = false;
+    while (!done && !eof) {
+        buf.assign(carry.begin(), carry.end());
+        const size_t have = buf.size();
+        buf.resize(have + kBlock);
+        const size_t got = std::fread(buf.data() + have, 1, kBlock, f);
+        buf.resize(have + got);
+        eof = got < kBlock;
+        // Complete lines of this block: up to the last newline (all of it at EOF).
+        size_t end = buf.size();
+        if (!eof) {
+            size_t nl = end;
+            while (nl > 0 && buf[nl - 1] != '\n') nl--;
+            if (nl == 0) {  // a line longer than the block: keep reading
+                carry.assign(buf.begin(), buf.end());
+                continue;
             }
-            cur = next;
-        } else if (tok.size() == 4) {
-            int32_t doc;
-            if (!parse_int(tok[3].first, tok[3].second, &doc)) { std::cout << "\nInvalid data: " << line << std::endl; continue; }
-            for (int r = 0; r < MC_MAX_SERP; r++)
-                if (cur.docs[r] == doc) { cur.click |= (uint16_t)(1u << r); break; }
-        } else {
-            std::cout << "\nInvalid data: " << line << std::endl;
+            end = nl;
         }
-        session_prev = sid;
-        have_prev = true;
+        carry.assign(buf.begin() + (long)end, buf.end());
+        if (end == 0) break;
+        const char* base = buf.data();
+        // Thread ranges start at line boundaries.
+        std::vector<size_t> cut(n_threads + 1, end);
+        cut[0] = 0;
+        for (unsigned t = 1; t < n_threads; t++) {
+            size_t c = std::max(cut[t - 1], end * t / n_threads);
+            while (c < end && c > 0 && base[c - 1] != '\n') c++;
+            cut[t] = c;
+        }
+        auto work = [&](unsigned t) {
+            std::vector<ParsedLine>& v = parts[t];
+            v.clear();
+            size_t p = cut[t];
+            const size_t e = cut[t + 1];
+            while (p < e) {
+                const char* nl = static_cast<const char*>(std::memchr(base + p, '\n', e - p));
+                const size_t q = nl ? (size_t)(nl - base) : e;
+                v.push_back(parse_line(base + p, base + q));
+                p = q + 1;
+            }
+        };
+        std::vector<std::thread> pool;
+        for (unsigned t = 1; t < n_threads; t++) pool.emplace_back(work, t);
+        work(0);
+        for (auto& th : pool) th.join();
+        for (unsigned t = 0; t < n_threads && !done; t++) {
+            for (const ParsedLine& pl : parts[t]) {
+                if (!(n_queries < max_sessions || max_sessions == -1)) { done = true; break; }
+                if (pl.kind == 0 || pl.kind == 3) std::cout << "\nInvalid data: " << std::string(pl.b, pl.e) << std::endl;
+                if (pl.kind == 0) continue;
+                if (pl.kind == 1) {
+                    if (have_prev && session_prev != -1) {
+                        query.push_back(cur.query);
+                        docs.insert(docs.end(), cur.docs, cur.docs + MC_MAX_SERP);
+                        click.push_back(cur.click);
+                        n_queries++;
+                    }
+                    cur = RawSession();
+                    cur.query = pl.query;
+                    std::memcpy(cur.docs, pl.v, sizeof(cur.docs));
+                } else if (pl.kind == 2) {
+                    for (int r = 0; r < MC_MAX_SERP; r++)
+                        if (cur.docs[r] == pl.v[0]) { cur.click |= (uint16_t)(1u << r); break; }
+                }
+                session_prev = pl.sid;
+                have_prev = true;
+            }
+        }
     }
+    std::fclose(f);
     mc_dataset* d = new (std::nothrow) mc_dataset();
     if (!d) return set_error(MC_ERR_NOMEM, "dataset_parse: out of host memory");
     build_partition(query, docs, click, test_share, d);
