@@ -297,8 +297,8 @@ def run_ours(args, rank: int, world: int, local: int):
     # ---- roofline of the fused kernel (one launch = one iteration) ----------
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs") or 6800.0
-    # Algorithmic bytes per launch, per unit as in the survey's hot-path table:
-    # per session int32 pidx x10 + uint16 click mask (42 B); per qd and private
+    # Algorithmic bytes per launch, the per-unit model of the reference's data
+    # path: per session int32 pidx x10 + uint16 click mask (42 B); per qd and private
     # parameter a 4 B value read, a 16 B FP64 statistic write and read and a
     # 4 B value write (DBN: two private parameters, 80 B).
     algo_bytes = 42 * n_train + 80 * n_qd
@@ -324,7 +324,7 @@ def run_ours(args, rank: int, world: int, local: int):
                 "traffic": traffic, "traffic_source": traffic_source,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks.get("hbm_gbs") else "fallback 6.8 TB/s",
                 "algorithmic_bytes_per_launch": algo_bytes,
-                "bytes_model": "42 B/session + 80 B/qd (DBN; survey hot-path table)",
+                "bytes_model": "42 B/session (int32 pidx x10 + uint16 clicks) + 80 B/qd (DBN: 2 private parameters x (4 B value read + 16 B FP64 statistic write + read + 4 B value write))",
                 "design_bytes_per_launch": design_bytes,
                 "dram_gbs_measured": (traffic / (ms / 1000.0) / 1e9) if traffic else None,
                 "dram_frac_measured": (traffic / (ms / 1000.0) / 1e9 / hbm) if traffic else None}

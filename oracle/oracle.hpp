@@ -3,8 +3,8 @@
 // A CPU restatement of the reference's (skip-th/MassiveClicks) CPU training
 // path: session ingest, the E-step of PBM / UBM / DBN / CCM, the parameter
 // reset and update, and the test-set evaluation.  Only tests, the smoke check
-// and the benchmark's CPU-baseline leg use it, as the checker or the timed CPU
-// baseline; the product never links it.
+// and the benchmark's CPU-baseline leg use it, to check results or as the timed
+// CPU baseline; the product never links it.
 //
 // Templated on the arithmetic type T.  With T = float and one thread it
 // evaluates every expression in the reference's order and precision, so its
