@@ -35,6 +35,12 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "EM session-iterations/s (20M sessions, DBN)"
+MODELS = {"pbm": 0, "ccm": 1, "dbn": 2, "ubm": 3}
+
+
+def metric_for(model: str) -> str:
+    """The headline metric for DBN; the same measurement for the other models."""
+    return METRIC if model == "dbn" else METRIC.replace("DBN", model.upper())
 UNIT = "session-iterations/s"
 DATA = ("synthetic: 20M sessions, 1M queries Zipf(1.0), 50-doc pools, top-10 shown, ground-truth CCM clicks "
         "(tau 0.6/0.3/0.2, relevance Beta(1,3)), seeded; test share 0.2")
@@ -59,6 +65,8 @@ def parse_args():
                     help="dbn20m: the headline DBN fit; batched: 256 mixed fits in one launch; "
                          "adjoint: EM against the gradient trainer")
     ap.add_argument("--batch-fits", type=int, default=256)
+    ap.add_argument("--model", choices=sorted(MODELS), default="dbn",
+                    help="click model of the 20M-session workload (dbn is the headline)")
     return ap.parse_args()
 
 
@@ -138,7 +146,7 @@ def cpu_sample(ds, n_sample: int) -> np.ndarray:
     return np.concatenate([np.arange(starts[g], ends[g]) for g in chosen]) if chosen else np.zeros(0, np.int64)
 
 
-def time_cpu_oracle(ds, idx: np.ndarray, iters: int, warmup: int, threads: int):
+def time_cpu_oracle(ds, idx: np.ndarray, iters: int, warmup: int, threads: int, model: int = 2):
     """The reference's CPU path (FP32 restatement, reference threading) on the
     training sessions idx (whole queries): seconds per iteration, one entry
     per step."""
@@ -146,7 +154,7 @@ def time_cpu_oracle(ds, idx: np.ndarray, iters: int, warmup: int, threads: int):
     sub = ds.train
     p = sub.pidx[idx]
     nq = int(p.max()) + 1 if len(idx) else 0
-    fit = bindings.OracleFit("f32", 2, 0, sub.query[idx], p, sub.click[idx], nq)
+    fit = bindings.OracleFit("f32", model, 0, sub.query[idx], p, sub.click[idx], nq)
     fit.run(warmup, threads)
     times = []
     for _ in range(iters):
@@ -234,14 +242,14 @@ def run_reference(args, rank: int, world: int):
     # sessions per step).
     idx = cpu_sample(ds, min(args.cpu_sample, max(50_000, 250_000_000 // max(1, args.steps))))
     n = len(idx)
-    times = time_cpu_oracle(ds, idx, args.steps, max(1, min(args.warmup, 2)), threads)
+    times = time_cpu_oracle(ds, idx, args.steps, max(1, min(args.warmup, 2)), threads, MODELS[args.model])
     total = sum(times)
     value = n * len(times) / total
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "impl": "reference", "metric": metric_for(args.model), "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": DATA,
-        "config": {"workload": "DBN EM, 20M sessions (16M train), one EM iteration per step; "
+        "config": {"workload": f"{args.model.upper()} EM, 20M sessions (16M train), one EM iteration per step; "
                                f"each step times a bounded sample of {n} training sessions",
                    "sessions": args.sessions, "train_sessions": len(ds.train), "sample_sessions": n,
                    "parallelism": f"{threads} host threads"},
@@ -263,7 +271,7 @@ def run_ours(args, rank: int, world: int, local: int):
     n_train, n_qd = len(ds.train), ds.n_qd
     stream = torch.cuda.Stream()
 
-    cm = api.DBNModel(device=local)
+    cm = api.ClickModel.create(MODELS[args.model], device=local)
     t0 = time.perf_counter()
     cm.upload(ds.train, n_qd, stream)
     cm.upload_test(ds.test, stream)
@@ -300,18 +308,19 @@ def run_ours(args, rank: int, world: int, local: int):
     # Algorithmic bytes per launch, the per-unit model of the reference's data
     # path: per session int32 pidx x10 + uint16 click mask (42 B); per qd and private
     # parameter a 4 B value read, a 16 B FP64 statistic write and read and a
-    # 4 B value write (DBN: two private parameters, 80 B).
-    algo_bytes = 42 * n_train + 80 * n_qd
+    # 4 B value write (40 B; DBN has two private parameters, 80 B).
+    per_qd = 80 if args.model == "dbn" else 40
+    algo_bytes = 42 * n_train + per_qd * n_qd
     achieved = algo_bytes / (ms / 1000.0) / 1e9
     # This design's own bytes: packed sessions that carry variable statistics
     # (22 B: uint16 window indices x10 + clicks) and per qd 24 B (atr, sat,
     # counts read; atr, sat written).
-    n_clicked = int(np.count_nonzero(ds.train.click))
-    design_bytes = 22 * n_clicked + 24 * n_qd
+    n_packed = int(np.count_nonzero(ds.train.click)) if args.model in ("dbn", "ccm") else n_train
+    design_bytes = 22 * n_packed + (24 if args.model == "dbn" else 16) * n_qd
     tr = profile_traffic()
     traffic = None
     traffic_source = None
-    if tr and tr.get("bytes_per_launch") and tr.get("n_train") and tr.get("n_qd"):
+    if args.model == "dbn" and tr and tr.get("bytes_per_launch") and tr.get("n_train") and tr.get("n_qd"):
         if tr["n_train"] == n_train and tr["n_qd"] == n_qd:
             traffic = tr["bytes_per_launch"]
             traffic_source = "ncu dram__bytes_read.sum + dram__bytes_write.sum, this workload"
@@ -324,7 +333,7 @@ def run_ours(args, rank: int, world: int, local: int):
                 "traffic": traffic, "traffic_source": traffic_source,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks.get("hbm_gbs") else "fallback 6.8 TB/s",
                 "algorithmic_bytes_per_launch": algo_bytes,
-                "bytes_model": "42 B/session (int32 pidx x10 + uint16 clicks) + 80 B/qd (DBN: 2 private parameters x (4 B value read + 16 B FP64 statistic write + read + 4 B value write))",
+                "bytes_model": f"42 B/session (int32 pidx x10 + uint16 clicks) + {per_qd} B/qd (per private parameter: 4 B value read + 16 B FP64 statistic write + read + 4 B value write)",
                 "design_bytes_per_launch": design_bytes,
                 "dram_gbs_measured": (traffic / (ms / 1000.0) / 1e9) if traffic else None,
                 "dram_frac_measured": (traffic / (ms / 1000.0) / 1e9 / hbm) if traffic else None}
@@ -376,7 +385,7 @@ def run_ours(args, rank: int, world: int, local: int):
 
         def e2e_step():
             m2 = C.c_void_p()
-            api.check(lib.mc_model_create(2, 0, local, C.byref(m2)))
+            api.check(lib.mc_model_create(MODELS[args.model], 0, local, C.byref(m2)))
             api.check(lib.mc_model_upload(m2, n_train, C.c_void_p(pq.data_ptr()), C.c_void_p(pp.data_ptr()),
                                           C.c_void_p(pm.data_ptr()), n_qd, C.c_void_p(stream.cuda_stream)))
             api.check(lib.mc_model_configure(m2, spt, wqd, block))
@@ -405,20 +414,20 @@ def run_ours(args, rank: int, world: int, local: int):
         threads = os.cpu_count() or 1
         idx = cpu_sample(ds, args.cpu_sample)
         n = len(idx)
-        times = time_cpu_oracle(ds, idx, 2, 1, threads)
+        times = time_cpu_oracle(ds, idx, 2, 1, threads, MODELS[args.model])
         cpu = {"value": n * len(times) / sum(times), "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{n} training sessions (whole queries), {len(times)} iterations after 1 warm-up; "
                          "FP32 restatement of the reference's CPU path with its threading"}
 
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "metric": metric_for(args.model), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": DATA,
-            "config": {"workload": "DBN EM over 16M training sessions (20M sessions, test share 0.2); "
+            "config": {"workload": f"{args.model.upper()} EM over 16M training sessions (20M sessions, test share 0.2); "
                                    "one fused kernel launch per iteration, replayed from a CUDA graph",
                        "sessions": args.sessions, "train_sessions": n_train, "n_qd": n_qd,
-                       "model": "DBN", "mode": "parity", "tile": {"sessions_per_tile": spt, "window_qd": wqd,
+                       "model": args.model.upper(), "mode": "parity", "tile": {"sessions_per_tile": spt, "window_qd": wqd,
                                                                    "block": block},
                        "l2": "inputs larger than L2 (sessions 672 MB + parameters), no flush",
                        "parallelism": "replicas" if world > 1 else "single GPU", "prep": prep},

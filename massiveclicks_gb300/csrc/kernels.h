@@ -16,6 +16,8 @@ cudaError_t fused_occupancy(int model, int block, size_t smem, int* blocks_per_s
 cudaError_t launch_em_fused(int model, const FitDev* fits, const TileDev* tiles, int n_tiles, const SplitDev* splits,
                             WorkState* ws, int window_max, int spt, int n_stages, int grid, int block,
                             cudaStream_t stream);
+// PBM iteration from unclicked-occurrence counts per (qd, rank) (em_counts.cu).
+cudaError_t launch_pbm_counts(const FitDev* fit, const uint32_t* ucnt, int64_t n_qd, int n_sm, cudaStream_t st);
 cudaError_t launch_pack_tiles(int model, TileDev* tiles, int n_tiles, int window_max, int max_tile_sessions, const int32_t* planes,
                               int64_t stride, const uint16_t* click, unsigned char* tblk, int* status, int n_sm,
                               cudaStream_t st);

@@ -80,7 +80,7 @@ __global__ void pairs_to_pub_kernel(const float2* pub2, float* theta, const int*
 __global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32_t* __restrict__ pidx_sm,
                             const uint16_t* __restrict__ click, const int32_t* __restrict__ seg_id,
                             int model, int32_t* planes, uint2* cnt, int* seg_lo, int* seg_hi,
-                            unsigned long long* pub_counts, uint32_t* packbits, int* flag) {
+                            unsigned long long* pub_counts, uint32_t* packbits, uint32_t* ucnt, int* flag) {
     __shared__ unsigned int sc[MC_PUB_COUNTS];
     for (int k = threadIdx.x; k < MC_PUB_COUNTS; k += blockDim.x) sc[k] = 0;
     __syncthreads();
@@ -118,6 +118,10 @@ __global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32
             if (valid && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
                 atomicAdd(reinterpret_cast<unsigned long long*>(cnt + p),
                           (unsigned long long)__popc(peers) | ((unsigned long long)__popc(clicked) << 32));
+            if (ucnt) {  // PBM: unclicked occurrences per (qd, rank), one atomic per distinct qd of the warp
+                const unsigned uncl = __popc(peers) - __popc(clicked);
+                if (valid && uncl && (int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(ucnt + (int64_t)p * MC_R + r, uncl);
+            }
             slot[r] = r * (r + 1) / 2 + last;
             if (c) last = r;
             if (model == 0) {  // clicks per rank, summed over the warp
@@ -268,6 +272,7 @@ struct mc_model {
     uint16_t* d_click = nullptr;
     uint2* d_cnt = nullptr;
     uint32_t* d_cnt16 = nullptr;
+    uint32_t* d_ucnt = nullptr;  // PBM: unclicked occurrences [n_qd][10], for the count kernel
     float *d_atr = nullptr, *d_sat = nullptr, *d_pub_theta = nullptr;
     double *d_pub_bins = nullptr, *d_pub_const = nullptr, *d_split_bins = nullptr;
     unsigned *d_split_count = nullptr, *d_tiles_done = nullptr;
@@ -336,7 +341,7 @@ struct mc_model {
         drop_graph();
         free_tiles();
         free_plain();
-        dfree(d_pidx); dfree(d_click); dfree(d_cnt); dfree(d_cnt16); dfree(d_atr); dfree(d_sat); dfree(d_pub_theta);
+        dfree(d_pidx); dfree(d_click); dfree(d_cnt); dfree(d_cnt16); dfree(d_ucnt); dfree(d_atr); dfree(d_sat); dfree(d_pub_theta);
         dfree(d_pub_bins); dfree(d_pub_const); dfree(d_tiles_done); dfree(d_iter); dfree(d_status);
         dfree(d_fit); dfree(d_ws); dfree(d_grad);
         bytes = test_bytes;
@@ -735,6 +740,7 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     const int64_t qd_alloc = m->qd_alloc();
     if ((rc = dalloc(&m->d_cnt, (size_t)qd_alloc, &B))) return fail_seg(rc);
     if ((rc = dalloc(&m->d_cnt16, (size_t)qd_alloc, &B))) return fail_seg(rc);
+    if (m->model == MC_PBM && (rc = dalloc(&m->d_ucnt, (size_t)qd_alloc * MC_R, &B))) return fail_seg(rc);
     if ((rc = dalloc(&m->d_atr, (size_t)qd_alloc, &B))) return fail_seg(rc);
     if (m->model == MC_DBN && (rc = dalloc(&m->d_sat, (size_t)qd_alloc, &B))) return fail_seg(rc);
     if ((rc = dalloc(&m->d_pub_theta, 2 * MC_MAX_PUB, &B))) return fail_seg(rc);
@@ -775,10 +781,11 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     ck(cudaMemsetAsync(d_pub_counts, 0, MC_PUB_COUNTS * 8, st));
     ck(cudaMemsetAsync(m->d_pidx, 0, (size_t)(m->stride * MC_R) * 4, st));
     ck(cudaMemsetAsync(m->d_cnt, 0, (size_t)qd_alloc * sizeof(uint2), st));
+    if (m->d_ucnt) ck(cudaMemsetAsync(m->d_ucnt, 0, (size_t)qd_alloc * MC_R * sizeof(uint32_t), st));
     if (n && e == cudaSuccess) {
         int grid = (int)std::min<int64_t>((n + 255) / 256, (int64_t)8 * m->n_sm);
         prep_kernel<<<grid, 256, 0, st>>>(n, m->stride, n_qd, d_src, m->d_click, d_seg_id, m->model,
-                                          m->d_pidx, m->d_cnt, d_seg_lo, d_seg_hi, d_pub_counts, d_packbits, d_flag);
+                                          m->d_pidx, m->d_cnt, d_seg_lo, d_seg_hi, d_pub_counts, d_packbits, m->d_ucnt, d_flag);
         ck(cudaGetLastError());
     }
     {
@@ -907,10 +914,16 @@ extern "C" int mc_model_get_config(const mc_model* m, int32_t* spt, int32_t* wqd
     return MC_OK;
 }
 
+// One fused iteration: PBM from its per-(qd, rank) counts, the other models
+// through the tile kernel.
+static cudaError_t launch_fused_once(mc_model* m, cudaStream_t st) {
+    if (m->d_ucnt) return launch_pbm_counts(m->d_fit, m->d_ucnt, m->n_qd, m->n_sm, st);
+    return launch_em_fused(m->model, m->d_fit, m->d_tiles, m->n_tiles, m->d_splits, m->d_ws, m->wqd, m->spt, m->stages,
+                           m->grid, m->block, st);
+}
+
 static int launch_fused_loop(mc_model* m, int iters, cudaStream_t st) {
-    for (int i = 0; i < iters; i++)
-        CK(launch_em_fused(m->model, m->d_fit, m->d_tiles, m->n_tiles, m->d_splits, m->d_ws, m->wqd, m->spt, m->stages,
-                           m->grid, m->block, st));
+    for (int i = 0; i < iters; i++) CK(launch_fused_once(m, st));
     return MC_OK;
 }
 
@@ -1143,8 +1156,7 @@ extern "C" int mc_model_em_trace(mc_model* m, int32_t iters, double* train_ll, v
     A.pub = m->d_pub_theta;
     A.iter = m->d_iter;  // the public half written by the iteration just run
     for (int i = 0; i < iters && e == cudaSuccess; i++) {
-        ck(launch_em_fused(m->model, m->d_fit, m->d_tiles, m->n_tiles, m->d_splits, m->d_ws, m->wqd, m->spt,
-                           m->stages, m->grid, m->block, st));
+        ck(launch_fused_once(m, st));
         A.out = d_trace + (int64_t)i * (MC_R + 1);
         ck(launch_eval(A, m->n_sm, st));
     }
