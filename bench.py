@@ -42,8 +42,13 @@ def metric_for(model: str) -> str:
     """The headline metric for DBN; the same measurement for the other models."""
     return METRIC if model == "dbn" else METRIC.replace("DBN", model.upper())
 UNIT = "session-iterations/s"
-DATA = ("synthetic: 20M sessions, 1M queries Zipf(1.0), 50-doc pools, top-10 shown, ground-truth CCM clicks "
-        "(tau 0.6/0.3/0.2, relevance Beta(1,3)), seeded; test share 0.2")
+def _count(n: int) -> str:
+    return f"{n / 1e6:g}M" if n >= 1_000_000 else f"{n:,}"
+
+
+def data_text(args) -> str:
+    return (f"synthetic: {_count(args.sessions)} sessions, {_count(args.queries)} queries Zipf(1.0), 50-doc pools, "
+            "top-10 shown, ground-truth CCM clicks (tau 0.6/0.3/0.2, relevance Beta(1,3)), seeded; test share 0.2")
 
 
 def parse_args():
@@ -248,8 +253,9 @@ def run_reference(args, rank: int, world: int):
     line = {
         "impl": "reference", "metric": metric_for(args.model), "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / len(times),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": DATA,
-        "config": {"workload": f"{args.model.upper()} EM, 20M sessions (16M train), one EM iteration per step; "
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": data_text(args),
+        "config": {"workload": f"{args.model.upper()} EM, {_count(args.sessions)} sessions ({_count(len(ds.train))} train), "
+                               "one EM iteration per step; "
                                f"each step times a bounded sample of {n} training sessions",
                    "sessions": args.sessions, "train_sessions": len(ds.train), "sample_sessions": n,
                    "parallelism": f"{threads} host threads"},
@@ -315,8 +321,16 @@ def run_ours(args, rank: int, world: int, local: int):
     # This design's own bytes: packed sessions that carry variable statistics
     # (22 B: uint16 window indices x10 + clicks) and per qd 24 B (atr, sat,
     # counts read; atr, sat written).
-    n_packed = int(np.count_nonzero(ds.train.click)) if args.model in ("dbn", "ccm") else n_train
-    design_bytes = 22 * n_packed + (24 if args.model == "dbn" else 16) * n_qd
+    path, n_entries = cm.fused_path()
+    if path == "counts":
+        # PBM/UBM count kernel: 4 B per count entry; per qd 4 B offset, 8 B
+        # occurrence/click counts, 4 B value read and 4 B value written.
+        design_bytes = 4 * n_entries + 20 * n_qd
+        design_model = f"count path: 4 B x {n_entries} entries + 20 B/qd"
+    else:
+        n_packed = int(np.count_nonzero(ds.train.click)) if args.model in ("dbn", "ccm") else n_train
+        design_bytes = 22 * n_packed + (24 if args.model == "dbn" else 16) * n_qd
+        design_model = f"tile path: 22 B x {n_packed} packed sessions + {24 if args.model == 'dbn' else 16} B/qd"
     tr = profile_traffic()
     traffic = None
     traffic_source = None
@@ -335,6 +349,7 @@ def run_ours(args, rank: int, world: int, local: int):
                 "algorithmic_bytes_per_launch": algo_bytes,
                 "bytes_model": f"42 B/session (int32 pidx x10 + uint16 clicks) + {per_qd} B/qd (per private parameter: 4 B value read + 16 B FP64 statistic write + read + 4 B value write)",
                 "design_bytes_per_launch": design_bytes,
+                "design_bytes_model": design_model,
                 "dram_gbs_measured": (traffic / (ms / 1000.0) / 1e9) if traffic else None,
                 "dram_frac_measured": (traffic / (ms / 1000.0) / 1e9 / hbm) if traffic else None}
 
@@ -423,8 +438,9 @@ def run_ours(args, rank: int, world: int, local: int):
         line = {
             "metric": metric_for(args.model), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": DATA,
-            "config": {"workload": f"{args.model.upper()} EM over 16M training sessions (20M sessions, test share 0.2); "
+            "vs_baseline": None, "dtype": "f32", "data": data_text(args),
+            "config": {"workload": f"{args.model.upper()} EM over {_count(n_train)} training sessions "
+                                   f"({_count(args.sessions)} sessions, test share 0.2); "
                                    "one fused kernel launch per iteration, replayed from a CUDA graph",
                        "sessions": args.sessions, "train_sessions": n_train, "n_qd": n_qd,
                        "model": args.model.upper(), "mode": "parity", "tile": {"sessions_per_tile": spt, "window_qd": wqd,

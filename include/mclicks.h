@@ -205,6 +205,13 @@ int mc_model_evaluate(mc_model* m, int which, double* ll_sum, double* log2_sums,
  * Synchronous. */
 int mc_model_em_trace(mc_model* m, int32_t n_iterations, double* train_ll, void* stream);
 
+/* Which kernel one fused iteration of the uploaded model launches: *path = 0
+ * the tile kernel over the sessions, 1 the count kernel over the per-(qd, key)
+ * occurrence counts built at upload (PBM and UBM); *n_entries = the number of
+ * count entries (0 on the tile path).  The reference has one E-step kernel per
+ * model (pbm.cu:191-253, ubm.cu:185-247); this reports which equivalent runs. */
+int mc_model_fused_path(const mc_model* m, int32_t* path, int64_t* n_entries);
+
 /* Device memory held by the model, in bytes. */
 int mc_model_memory(const mc_model* m, int64_t* bytes);
 

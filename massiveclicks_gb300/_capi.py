@@ -57,6 +57,7 @@ _SIGS = {
     "mc_model_set_param": (C.c_int, [_VP, C.c_int, _VP, _VP]),
     "mc_model_evaluate": (C.c_int, [_VP, C.c_int, C.POINTER(_F64), _VP, C.POINTER(_I64), _VP]),
     "mc_model_em_trace": (C.c_int, [_VP, C.c_int32, _VP, _VP]),
+    "mc_model_fused_path": (C.c_int, [_VP, C.POINTER(C.c_int32), C.POINTER(_I64)]),
     "mc_model_memory": (C.c_int, [_VP, C.POINTER(_I64)]),
     "mc_model_destroy": (None, [_VP]),
     "mc_batch_create": (C.c_int, [C.c_int, _VP, C.POINTER(_VP)]),

@@ -266,6 +266,14 @@ class ClickModel:
         rank_ppl = [2.0 ** (-l2[r] / nn) for r in range(R)]
         return Evaluation(ll.value / nn, sum(rank_ppl) / R, rank_ppl, nn, ll.value, l2)
 
+    def fused_path(self) -> tuple:
+        """("tiles", 0) when a fused iteration runs the tile kernel over the
+        sessions, ("counts", n_entries) when it runs the count kernel over the
+        per-(qd, key) occurrence counts (PBM and UBM)."""
+        p, n = C.c_int32(), C.c_int64()
+        check(_capi.load().mc_model_fused_path(self._h, C.byref(p), C.byref(n)))
+        return ("counts" if p.value == 1 else "tiles", int(n.value))
+
     def memory(self) -> int:
         b = C.c_int64()
         check(_capi.load().mc_model_memory(self._h, C.byref(b)))

@@ -16,8 +16,14 @@ cudaError_t fused_occupancy(int model, int block, size_t smem, int* blocks_per_s
 cudaError_t launch_em_fused(int model, const FitDev* fits, const TileDev* tiles, int n_tiles, const SplitDev* splits,
                             WorkState* ws, int window_max, int spt, int n_stages, int grid, int block,
                             cudaStream_t stream);
-// PBM iteration from unclicked-occurrence counts per (qd, rank) (em_counts.cu).
-cudaError_t launch_pbm_counts(const FitDev* fit, const uint32_t* ucnt, int64_t n_qd, int n_sm, cudaStream_t st);
+// PBM/UBM iterations from counts per (qd, statistic key) (em_counts.cu).
+// build_counts sorts the unclicked occurrences of the uploaded sessions into
+// per-qd entries (CSR: off[n_qd + 1], ent[n_entries]); *usable = 0 keeps the
+// tile path (sizes beyond the entry format).
+cudaError_t build_counts(int model, int64_t n, int64_t stride, int64_t n_qd, const int32_t* planes, const uint16_t* click,
+                         int n_sm, cudaStream_t st, uint32_t** off, uint32_t** ent, int64_t* n_entries, int* usable);
+cudaError_t launch_em_counts(const FitDev* fit, const uint32_t* off, const uint32_t* ent, int64_t n_qd, int n_sm,
+                             cudaStream_t st);
 cudaError_t launch_pack_tiles(int model, TileDev* tiles, int n_tiles, int window_max, int max_tile_sessions, const int32_t* planes,
                               int64_t stride, const uint16_t* click, unsigned char* tblk, int* status, int n_sm,
                               cudaStream_t st);

@@ -80,7 +80,7 @@ __global__ void pairs_to_pub_kernel(const float2* pub2, float* theta, const int*
 __global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32_t* __restrict__ pidx_sm,
                             const uint16_t* __restrict__ click, const int32_t* __restrict__ seg_id,
                             int model, int32_t* planes, uint2* cnt, int* seg_lo, int* seg_hi,
-                            unsigned long long* pub_counts, uint32_t* packbits, uint32_t* ucnt, int* flag) {
+                            unsigned long long* pub_counts, uint32_t* packbits, int* flag) {
     __shared__ unsigned int sc[MC_PUB_COUNTS];
     for (int k = threadIdx.x; k < MC_PUB_COUNTS; k += blockDim.x) sc[k] = 0;
     __syncthreads();
@@ -118,10 +118,7 @@ __global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32
             if (valid && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
                 atomicAdd(reinterpret_cast<unsigned long long*>(cnt + p),
                           (unsigned long long)__popc(peers) | ((unsigned long long)__popc(clicked) << 32));
-            if (ucnt) {  // PBM: unclicked occurrences per (qd, rank), one atomic per distinct qd of the warp
-                const unsigned uncl = __popc(peers) - __popc(clicked);
-                if (valid && uncl && (int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(ucnt + (int64_t)p * MC_R + r, uncl);
-            }
+
             slot[r] = r * (r + 1) / 2 + last;
             if (c) last = r;
             if (model == 0) {  // clicks per rank, summed over the warp
@@ -272,7 +269,9 @@ struct mc_model {
     uint16_t* d_click = nullptr;
     uint2* d_cnt = nullptr;
     uint32_t* d_cnt16 = nullptr;
-    uint32_t* d_ucnt = nullptr;  // PBM: unclicked occurrences [n_qd][10], for the count kernel
+    uint32_t* d_coff = nullptr;  // PBM/UBM: per-qd entry offsets [n_qd + 1] of the count path
+    uint32_t* d_cent = nullptr;  // PBM/UBM: entries (count << 7 | key << 1 | alive)
+    int64_t n_cent = 0;
     float *d_atr = nullptr, *d_sat = nullptr, *d_pub_theta = nullptr;
     double *d_pub_bins = nullptr, *d_pub_const = nullptr, *d_split_bins = nullptr;
     unsigned *d_split_count = nullptr, *d_tiles_done = nullptr;
@@ -341,10 +340,11 @@ struct mc_model {
         drop_graph();
         free_tiles();
         free_plain();
-        dfree(d_pidx); dfree(d_click); dfree(d_cnt); dfree(d_cnt16); dfree(d_ucnt); dfree(d_atr); dfree(d_sat); dfree(d_pub_theta);
+        dfree(d_pidx); dfree(d_click); dfree(d_cnt); dfree(d_cnt16); dfree(d_coff); dfree(d_cent); dfree(d_atr); dfree(d_sat); dfree(d_pub_theta);
         dfree(d_pub_bins); dfree(d_pub_const); dfree(d_tiles_done); dfree(d_iter); dfree(d_status);
         dfree(d_fit); dfree(d_ws); dfree(d_grad);
         bytes = test_bytes;
+        n_cent = 0;
         uploaded = false;
     }
 
@@ -740,7 +740,6 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     const int64_t qd_alloc = m->qd_alloc();
     if ((rc = dalloc(&m->d_cnt, (size_t)qd_alloc, &B))) return fail_seg(rc);
     if ((rc = dalloc(&m->d_cnt16, (size_t)qd_alloc, &B))) return fail_seg(rc);
-    if (m->model == MC_PBM && (rc = dalloc(&m->d_ucnt, (size_t)qd_alloc * MC_R, &B))) return fail_seg(rc);
     if ((rc = dalloc(&m->d_atr, (size_t)qd_alloc, &B))) return fail_seg(rc);
     if (m->model == MC_DBN && (rc = dalloc(&m->d_sat, (size_t)qd_alloc, &B))) return fail_seg(rc);
     if ((rc = dalloc(&m->d_pub_theta, 2 * MC_MAX_PUB, &B))) return fail_seg(rc);
@@ -781,11 +780,10 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     ck(cudaMemsetAsync(d_pub_counts, 0, MC_PUB_COUNTS * 8, st));
     ck(cudaMemsetAsync(m->d_pidx, 0, (size_t)(m->stride * MC_R) * 4, st));
     ck(cudaMemsetAsync(m->d_cnt, 0, (size_t)qd_alloc * sizeof(uint2), st));
-    if (m->d_ucnt) ck(cudaMemsetAsync(m->d_ucnt, 0, (size_t)qd_alloc * MC_R * sizeof(uint32_t), st));
     if (n && e == cudaSuccess) {
         int grid = (int)std::min<int64_t>((n + 255) / 256, (int64_t)8 * m->n_sm);
         prep_kernel<<<grid, 256, 0, st>>>(n, m->stride, n_qd, d_src, m->d_click, d_seg_id, m->model,
-                                          m->d_pidx, m->d_cnt, d_seg_lo, d_seg_hi, d_pub_counts, d_packbits, m->d_ucnt, d_flag);
+                                          m->d_pidx, m->d_cnt, d_seg_lo, d_seg_hi, d_pub_counts, d_packbits, d_flag);
         ck(cudaGetLastError());
     }
     {
@@ -808,6 +806,20 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     if (flag) {
         m->free_train();
         return set_error(MC_ERR_INVALID, "model_upload: a parameter index is outside [0, n_qd)");
+    }
+    if ((m->model == MC_PBM || m->model == MC_UBM) && n) {
+        int usable = 0;
+        int64_t n_ent = 0;
+        e = build_counts(m->model, n, m->stride, n_qd, m->d_pidx, m->d_click, m->n_sm, st, &m->d_coff, &m->d_cent,
+                         &n_ent, &usable);
+        if (e != cudaSuccess) {
+            m->free_train();
+            return cuda_fail("model_upload", e);
+        }
+        if (usable) {
+            m->n_cent = n_ent;
+            m->bytes += (int64_t)sizeof(uint32_t) * ((n_qd + 1) + std::max<int64_t>(n_ent, 1));
+        }
     }
 
     // Fused path precondition: per-query qd ranges disjoint and increasing.
@@ -859,6 +871,9 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     CK(cudaMemsetAsync(m->d_ws, 0, sizeof(WorkState), st));
     CK(cudaStreamSynchronize(st));
     m->uploaded = true;
+    // The count path (PBM/UBM) reads the fit descriptor whether or not the
+    // sessions admit tiles; build_tiles rewrites it with the tile fields.
+    if ((rc = m->write_fit_desc())) return rc;
     if (m->fused_ok && (rc = m->build_tiles())) return rc;
     return MC_OK;
 }
@@ -914,10 +929,10 @@ extern "C" int mc_model_get_config(const mc_model* m, int32_t* spt, int32_t* wqd
     return MC_OK;
 }
 
-// One fused iteration: PBM from its per-(qd, rank) counts, the other models
-// through the tile kernel.
+// One fused iteration: PBM and UBM from their per-(qd, key) counts, the
+// other models (or sizes beyond the count format) through the tile kernel.
 static cudaError_t launch_fused_once(mc_model* m, cudaStream_t st) {
-    if (m->d_ucnt) return launch_pbm_counts(m->d_fit, m->d_ucnt, m->n_qd, m->n_sm, st);
+    if (m->d_coff) return launch_em_counts(m->d_fit, m->d_coff, m->d_cent, m->n_qd, m->n_sm, st);
     return launch_em_fused(m->model, m->d_fit, m->d_tiles, m->n_tiles, m->d_splits, m->d_ws, m->wqd, m->spt, m->stages,
                            m->grid, m->block, st);
 }
@@ -936,7 +951,9 @@ extern "C" int mc_model_em(mc_model* m, int32_t iters, int impl, void* stream) {
     cudaStream_t st = m->pick(stream);
     if (iters == 0 || m->n == 0) return MC_OK;
     if (impl == MC_IMPL_FUSED) {
-        if (!m->fused_ok) return set_error(MC_ERR_INVALID, "model_em: fused path unavailable: " + m->fused_reason);
+        // The count path (PBM/UBM) does not depend on the session order.
+        if (!m->fused_ok && !m->d_coff)
+            return set_error(MC_ERR_INVALID, "model_em: fused path unavailable: " + m->fused_reason);
         // The loop is captured as graphs of at most kGraphChunk iterations
         // (one full chunk, one remainder), each replayed as often as needed.
         const int full = iters / kGraphChunk, rem = iters % kGraphChunk;
@@ -1128,7 +1145,8 @@ extern "C" int mc_model_em_trace(mc_model* m, int32_t iters, double* train_ll, v
     if (!m->uploaded) return set_error(MC_ERR_STATE, "em_trace: no training sessions uploaded");
     if (iters < 0) return set_error(MC_ERR_INVALID, "em_trace: negative iteration count");
     if (iters > 0 && !train_ll) return set_error(MC_ERR_INVALID, "em_trace: null output");
-    if (!m->fused_ok) return set_error(MC_ERR_INVALID, "em_trace: fused path unavailable: " + m->fused_reason);
+    if (!m->fused_ok && !m->d_coff)
+        return set_error(MC_ERR_INVALID, "em_trace: fused path unavailable: " + m->fused_reason);
     CK(cudaSetDevice(m->device));
     cudaStream_t st = m->pick(stream);
     if (iters == 0) return MC_OK;
@@ -1212,6 +1230,14 @@ extern "C" int mc_model_autotune(mc_model* m, void* stream) {
     CK(cudaMemcpy(m->d_pub_theta, th.data(), th.size() * 4, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(m->d_iter, &it0, 4, cudaMemcpyHostToDevice));
     return check_status(m, st);
+}
+
+extern "C" int mc_model_fused_path(const mc_model* m, int32_t* path, int64_t* n_entries) {
+    if (!m || !path || !n_entries) return set_error(MC_ERR_INVALID, "model_fused_path: null argument");
+    if (!m->uploaded) return set_error(MC_ERR_STATE, "model_fused_path: no training sessions uploaded");
+    *path = m->d_coff ? 1 : 0;
+    *n_entries = m->d_coff ? m->n_cent : 0;
+    return MC_OK;
 }
 
 extern "C" int mc_model_memory(const mc_model* m, int64_t* bytes) {
