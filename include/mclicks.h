@@ -150,7 +150,8 @@ int mc_model_configure(mc_model* m, int32_t sessions_per_tile, int32_t window_qd
 int mc_model_get_config(const mc_model* m, int32_t* sessions_per_tile, int32_t* window_qd, int32_t* block_size);
 
 /* Times a few fused iterations for each tile shape of a small grid and keeps
- * the fastest.  Parameters are restored afterwards. */
+ * the fastest.  Parameters are restored afterwards.  A model on the count path
+ * (mc_model_fused_path: PBM, UBM) has no tile shape to tune and returns at once. */
 int mc_model_autotune(mc_model* m, void* stream);
 
 /* Runs n_iterations EM iterations: replaces the loop of em_parallel
@@ -214,6 +215,13 @@ int mc_model_fused_path(const mc_model* m, int32_t* path, int64_t* n_entries);
 
 /* Device memory held by the model, in bytes. */
 int mc_model_memory(const mc_model* m, int64_t* bytes);
+
+/* Device blocks the library freed are kept in a per-device cache and handed
+ * out again (models created and destroyed with the same sizes then skip
+ * cudaMalloc / cudaFree).  mc_empty_cache frees the cached blocks of one device
+ * (-1: all) back to the driver; mc_cache_bytes reports how much is cached. */
+int mc_empty_cache(int device, int64_t* bytes_released);
+int mc_cache_bytes(int device, int64_t* bytes);
 
 /* Replaces destroy_parameters (pbm.cu:445-460 etc.). */
 void mc_model_destroy(mc_model* m);

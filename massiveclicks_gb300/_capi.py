@@ -59,6 +59,8 @@ _SIGS = {
     "mc_model_em_trace": (C.c_int, [_VP, C.c_int32, _VP, _VP]),
     "mc_model_fused_path": (C.c_int, [_VP, C.POINTER(C.c_int32), C.POINTER(_I64)]),
     "mc_model_memory": (C.c_int, [_VP, C.POINTER(_I64)]),
+    "mc_empty_cache": (C.c_int, [C.c_int, C.POINTER(_I64)]),
+    "mc_cache_bytes": (C.c_int, [C.c_int, C.POINTER(_I64)]),
     "mc_model_destroy": (None, [_VP]),
     "mc_batch_create": (C.c_int, [C.c_int, _VP, C.POINTER(_VP)]),
     "mc_batch_em": (C.c_int, [_VP, _I32, _VP]),

@@ -336,6 +336,21 @@ class Batch:
             pass
 
 
+def empty_cache(device: int = -1) -> int:
+    """Frees the device blocks the library keeps for reuse (one device, or all
+    with -1) and returns the bytes released."""
+    b = C.c_int64()
+    check(_capi.load().mc_empty_cache(int(device), C.byref(b)))
+    return int(b.value)
+
+
+def cache_bytes(device: int = -1) -> int:
+    """Bytes of freed device blocks the library keeps for reuse."""
+    b = C.c_int64()
+    check(_capi.load().mc_cache_bytes(int(device), C.byref(b)))
+    return int(b.value)
+
+
 def em_parallel(model_type: int, dataset: Dataset, iterations: int = 50, mode: int = MODE_PARITY,
                 impl: int = IMPL_FUSED, device: int = 0) -> tuple[ClickModel, Evaluation]:
     """em_parallel (parallel_em/parallel_em.cu:349-746) for one GPU: upload,

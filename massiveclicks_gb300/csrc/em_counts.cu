@@ -24,17 +24,20 @@
 #include <cub/device/device_run_length_encode.cuh>
 
 #include "common.cuh"
+#include "devmem.h"
 #include "kernels.h"
 
 namespace mcd {
 
-constexpr unsigned long long kNoKey = ~0ull;  // clicked occurrence: sorts after every key
-constexpr uint32_t kMaxCount = 1u << 25;      // count field of an entry
+constexpr uint32_t kMaxCount = 1u << 25;  // count field of an entry
 
-// Keys ((qd << 7) | (k << 1) | alive) of the unclicked occurrences of sessions
-// [0, n); position s * 10 + r.
+// Keys ((qd << 7) | (k << 1) | alive) of the unclicked occurrences; a clicked
+// occurrence gets the all-ones key, which sorts after every real key.  The key
+// of (session s, rank r) sits at r * n + s: the sort does not care where a key
+// starts, and rank-major positions make the stores coalesced.
+template <class K>
 __global__ void count_keys_kernel(int64_t n, int64_t stride, const int32_t* __restrict__ planes,
-                                  const uint16_t* __restrict__ click, int model, unsigned long long* __restrict__ keys) {
+                                  const uint16_t* __restrict__ click, int model, K* __restrict__ keys) {
     const int64_t step = (int64_t)gridDim.x * blockDim.x;
     for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += step) {
         const unsigned m = click[s];
@@ -47,41 +50,43 @@ __global__ void count_keys_kernel(int64_t n, int64_t stride, const int32_t* __re
         }
 #pragma unroll
         for (int r = 0; r < MC_R; r++) {
-            unsigned long long key = kNoKey;
+            K key = ~K(0);
             if (!((m >> r) & 1u)) {
                 bool alive = true;
 #pragma unroll
                 for (int r2 = r + 1; r2 < MC_R; r2++) alive = alive && slot[r2] != slot[r];
-                const int64_t p = planes[(int64_t)r * stride + s];
-                key = ((unsigned long long)p << 7) | ((unsigned long long)slot[r] << 1) | (alive ? 1ull : 0ull);
+                const K p = (K)planes[(int64_t)r * stride + s];
+                key = (p << 7) | ((K)slot[r] << 1) | (alive ? K(1) : K(0));
             }
-            keys[s * MC_R + r] = key;
+            keys[(int64_t)r * n + s] = key;
         }
     }
 }
 
 // Entry i = (count << 7) | (k << 1) | alive of run i; flags a count too large.
-__global__ void count_entries_kernel(int64_t runs, const unsigned long long* __restrict__ uniq,
-                                     const uint32_t* __restrict__ counts, uint32_t* __restrict__ ent, int* overflow) {
+template <class K>
+__global__ void count_entries_kernel(int64_t runs, const K* __restrict__ uniq, const uint32_t* __restrict__ counts,
+                                     uint32_t* __restrict__ ent, int* overflow) {
     const int64_t step = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < runs; i += step) {
         const uint32_t c = counts[i];
         if (c >= kMaxCount) atomicOr(overflow, 1);
-        ent[i] = (c << 7) | (uint32_t)(uniq[i] & 0x7Full);
+        ent[i] = (c << 7) | (uint32_t)(uniq[i] & K(0x7F));
     }
 }
 
-// off[q] = first run whose qd is >= q, q in [0, n_qd].
-__global__ void count_offsets_kernel(int64_t n_qd, int64_t runs, const unsigned long long* __restrict__ uniq,
-                                     uint32_t* __restrict__ off) {
+// off[q] = first run whose qd is >= q, for q in [0, n_qd]: run i writes the
+// offsets from just after the previous run's qd up to its own qd, and the last
+// run also those after its qd.  (off starts zeroed, which covers no runs.)
+template <class K>
+__global__ void count_offsets_kernel(int64_t n_qd, int64_t runs, const K* __restrict__ uniq, uint32_t* __restrict__ off) {
     const int64_t step = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q <= n_qd; q += step) {
-        int64_t lo = 0, hi = runs;
-        while (lo < hi) {
-            const int64_t mid = (lo + hi) / 2;
-            if ((int64_t)(uniq[mid] >> 7) < q) lo = mid + 1; else hi = mid;
-        }
-        off[q] = (uint32_t)lo;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < runs; i += step) {
+        const int64_t q = (int64_t)(uniq[i] >> 7);
+        const int64_t qp = i ? (int64_t)(uniq[i - 1] >> 7) : -1;
+        for (int64_t x = qp + 1; x <= q; x++) off[x] = (uint32_t)i;
+        if (i == runs - 1)
+            for (int64_t x = q + 1; x <= n_qd; x++) off[x] = (uint32_t)runs;
     }
 }
 
@@ -93,7 +98,83 @@ static int grid_for(int64_t n, int n_sm) {
 
 template <class T>
 static cudaError_t tmp_alloc(T** p, size_t count) {
-    return cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T) > 0 ? count * sizeof(T) : 1);
+    return mch::dev_alloc(reinterpret_cast<void**>(p), count * sizeof(T) > 0 ? count * sizeof(T) : 1);
+}
+
+// K = uint32_t while qd < 2^25 - 1 (the all-ones key stays above every real
+// key), else uint64_t.  The sort runs over the low end_bit bits, the fewest
+// that hold every real key below 2^end_bit - 1.
+template <class K>
+static cudaError_t build_counts_t(int model, int64_t n, int64_t stride, int64_t n_qd, const int32_t* planes,
+                                  const uint16_t* click, int n_sm, cudaStream_t st, uint32_t** off_out,
+                                  uint32_t** ent_out, int64_t* n_entries, int* usable) {
+    const int64_t nk = n * MC_R;
+    K *keys = nullptr, *alt = nullptr;
+    uint32_t* counts = nullptr;
+    int64_t* d_small = nullptr;  // [0] run count, [1] overflow flag
+    void* temp = nullptr;
+    uint32_t *off = nullptr, *ent = nullptr;
+    cudaError_t e = cudaSuccess;
+    auto ck = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+    auto release = [&]() {  // after the stream has drained
+        cudaStreamSynchronize(st);
+        mch::dev_free(keys); mch::dev_free(alt); mch::dev_free(counts); mch::dev_free(d_small); mch::dev_free(temp);
+    };
+    int end_bit = 8;
+    while (end_bit < (int)(8 * sizeof(K)) && (((int64_t)1 << (end_bit - 7)) - 1) < n_qd) end_bit++;
+    ck(tmp_alloc(&keys, (size_t)nk));
+    ck(tmp_alloc(&alt, (size_t)nk));
+    ck(tmp_alloc(&counts, (size_t)nk));
+    ck(tmp_alloc(&d_small, 2));
+    size_t sort_bytes = 0, rle_bytes = 0;
+    cub::DoubleBuffer<K> db(keys, alt);
+    if (e == cudaSuccess) {
+        ck(cub::DeviceRadixSort::SortKeys(nullptr, sort_bytes, db, (int64_t)nk, 0, end_bit, st));
+        ck(cub::DeviceRunLengthEncode::Encode(nullptr, rle_bytes, keys, alt, counts, d_small, (int64_t)nk, st));
+        ck(mch::dev_alloc(&temp, sort_bytes > rle_bytes ? sort_bytes : rle_bytes));
+    }
+    if (e != cudaSuccess) { release(); return e; }
+    ck(cudaMemsetAsync(d_small, 0, 16, st));
+    count_keys_kernel<K><<<grid_for(n, n_sm), 256, 0, st>>>(n, stride, planes, click, model, keys);
+    ck(cudaGetLastError());
+    ck(cub::DeviceRadixSort::SortKeys(temp, sort_bytes, db, (int64_t)nk, 0, end_bit, st));
+    K* sorted = db.Current();
+    K* uniq = db.Alternate();
+    ck(cub::DeviceRunLengthEncode::Encode(temp, rle_bytes, sorted, uniq, counts, d_small, (int64_t)nk, st));
+    int64_t runs = 0;
+    ck(cudaMemcpyAsync(&runs, d_small, 8, cudaMemcpyDeviceToHost, st));
+    ck(cudaStreamSynchronize(st));
+    if (e != cudaSuccess) { release(); return e; }
+    // The clicked occurrences form the last run (the all-ones key), if any.
+    if (runs > 0) {
+        K last_key = 0;
+        ck(cudaMemcpy(&last_key, uniq + runs - 1, sizeof(K), cudaMemcpyDeviceToHost));
+        if (last_key == ~K(0)) runs--;
+    }
+    ck(tmp_alloc(&off, (size_t)n_qd + 1));
+    ck(tmp_alloc(&ent, (size_t)(runs > 0 ? runs : 1)));
+    if (e == cudaSuccess) {
+        ck(cudaMemsetAsync(off, 0, ((size_t)n_qd + 1) * sizeof(uint32_t), st));
+        int* overflow = reinterpret_cast<int*>(d_small + 1);
+        count_entries_kernel<K><<<grid_for(runs, n_sm), 256, 0, st>>>(runs, uniq, counts, ent, overflow);
+        ck(cudaGetLastError());
+        count_offsets_kernel<K><<<grid_for(runs, n_sm), 256, 0, st>>>(n_qd, runs, uniq, off);
+        ck(cudaGetLastError());
+    }
+    int overflow = 0;
+    ck(cudaMemcpyAsync(&overflow, d_small + 1, 4, cudaMemcpyDeviceToHost, st));
+    ck(cudaStreamSynchronize(st));
+    release();
+    if (e != cudaSuccess || overflow) {
+        mch::dev_free(off);
+        mch::dev_free(ent);
+        return e;  // on overflow: success without the count path
+    }
+    *off_out = off;
+    *ent_out = ent;
+    *n_entries = runs;
+    *usable = 1;
+    return cudaSuccess;
 }
 
 cudaError_t build_counts(int model, int64_t n, int64_t stride, int64_t n_qd, const int32_t* planes, const uint16_t* click,
@@ -103,73 +184,11 @@ cudaError_t build_counts(int model, int64_t n, int64_t stride, int64_t n_qd, con
     *ent_out = nullptr;
     *n_entries = 0;
     *usable = 0;
-    const int64_t nk = n * MC_R;
-    if (nk >= ((int64_t)1 << 32) || n_qd >= ((int64_t)1 << 56)) return cudaSuccess;  // keep the tile path
-    unsigned long long *keys = nullptr, *sorted = nullptr, *uniq = nullptr;
-    uint32_t* counts = nullptr;
-    int* d_small = nullptr;  // [0] overflow flag, [1..2] run count (int64)
-    void* temp = nullptr;
-    uint32_t *off = nullptr, *ent = nullptr;
-    cudaError_t e = cudaSuccess;
-    auto ck = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-    auto release = [&]() {
-        cudaFree(keys); cudaFree(sorted); cudaFree(uniq); cudaFree(counts); cudaFree(d_small); cudaFree(temp);
-    };
-    // Real keys are below 2^end_bit - 1 once 2^(end_bit - 7) - 1 >= n_qd, so
-    // the sentinel (all ones) still sorts last on the low end_bit bits.
-    int end_bit = 8;
-    while (end_bit < 64 && (((int64_t)1 << (end_bit - 7)) - 1) < n_qd) end_bit++;
-    ck(tmp_alloc(&keys, (size_t)nk));
-    ck(tmp_alloc(&sorted, (size_t)nk));
-    ck(tmp_alloc(&uniq, (size_t)nk));
-    ck(tmp_alloc(&counts, (size_t)nk));
-    ck(tmp_alloc(&d_small, 4));
-    size_t sort_bytes = 0, rle_bytes = 0;
-    if (e == cudaSuccess) {
-        ck(cub::DeviceRadixSort::SortKeys(nullptr, sort_bytes, keys, sorted, (int64_t)nk, 0, end_bit, st));
-        ck(cub::DeviceRunLengthEncode::Encode(nullptr, rle_bytes, sorted, uniq, counts,
-                                              reinterpret_cast<int64_t*>(d_small + 2), (int64_t)nk, st));
-        ck(cudaMalloc(&temp, sort_bytes > rle_bytes ? sort_bytes : rle_bytes));
-    }
-    if (e != cudaSuccess) { release(); return e; }
-    ck(cudaMemsetAsync(d_small, 0, 16, st));
-    count_keys_kernel<<<grid_for(n, n_sm), 256, 0, st>>>(n, stride, planes, click, model, keys);
-    ck(cudaGetLastError());
-    ck(cub::DeviceRadixSort::SortKeys(temp, sort_bytes, keys, sorted, (int64_t)nk, 0, end_bit, st));
-    ck(cub::DeviceRunLengthEncode::Encode(temp, rle_bytes, sorted, uniq, counts,
-                                          reinterpret_cast<int64_t*>(d_small + 2), (int64_t)nk, st));
-    int64_t runs = 0;
-    ck(cudaMemcpyAsync(&runs, d_small + 2, 8, cudaMemcpyDeviceToHost, st));
-    ck(cudaStreamSynchronize(st));
-    if (e != cudaSuccess) { release(); return e; }
-    // The clicked occurrences form the last run (the sentinel), if any.
-    unsigned long long last_key = 0;
-    if (runs > 0) {
-        ck(cudaMemcpy(&last_key, uniq + runs - 1, 8, cudaMemcpyDeviceToHost));
-        if (last_key == kNoKey) runs--;
-    }
-    ck(tmp_alloc(&off, (size_t)n_qd + 1));
-    ck(tmp_alloc(&ent, (size_t)(runs > 0 ? runs : 1)));
-    if (e == cudaSuccess) {
-        count_entries_kernel<<<grid_for(runs, n_sm), 256, 0, st>>>(runs, uniq, counts, ent, d_small);
-        ck(cudaGetLastError());
-        count_offsets_kernel<<<grid_for(n_qd + 1, n_sm), 256, 0, st>>>(n_qd, runs, uniq, off);
-        ck(cudaGetLastError());
-    }
-    int overflow = 0;
-    ck(cudaMemcpyAsync(&overflow, d_small, 4, cudaMemcpyDeviceToHost, st));
-    ck(cudaStreamSynchronize(st));
-    release();
-    if (e != cudaSuccess || overflow) {
-        cudaFree(off);
-        cudaFree(ent);
-        return e;  // on overflow: success without the count path
-    }
-    *off_out = off;
-    *ent_out = ent;
-    *n_entries = runs;
-    *usable = 1;
-    return cudaSuccess;
+    if (n * MC_R >= ((int64_t)1 << 32) || n_qd >= ((int64_t)1 << 56)) return cudaSuccess;  // keep the tile path
+    if (n_qd <= ((int64_t)1 << 25) - 2)
+        return build_counts_t<uint32_t>(model, n, stride, n_qd, planes, click, n_sm, st, off_out, ent_out, n_entries, usable);
+    return build_counts_t<unsigned long long>(model, n, stride, n_qd, planes, click, n_sm, st, off_out, ent_out, n_entries,
+                                              usable);
 }
 
 // One thread per qd: its entries, its M-step in place; the public terms of the

@@ -24,6 +24,7 @@
 
 #include "mclicks.h"
 #include "host_internal.h"
+#include "devmem.h"
 #include "common.cuh"
 #include "kernels.h"
 
@@ -48,16 +49,24 @@ template <typename T>
 int dalloc(T** p, size_t count, int64_t* bytes) {
     *p = nullptr;
     if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    cudaError_t e = mch::dev_alloc((void**)p, count * sizeof(T));
     if (e != cudaSuccess) return cuda_fail("cudaMalloc", e);
     *bytes += (int64_t)(count * sizeof(T));
     return MC_OK;
 }
 
+// Back to the device cache: no work may be pending on p (see settle()).
 template <typename T>
 void dfree(T*& p) {
-    if (p) cudaFree((void*)p);
+    mch::dev_free((void*)p);
     p = nullptr;
+}
+
+// Waits for the device before buffers that kernels may still use are freed
+// (what cudaFree itself would wait for).
+template <typename... T>
+void settle(T*... ps) {
+    if (((ps != nullptr) || ...)) cudaDeviceSynchronize();
 }
 
 __global__ void pub_to_pairs_kernel(const float* theta, const int* iter, float2* pub2, int n_pub) {
@@ -77,29 +86,61 @@ __global__ void pairs_to_pub_kernel(const float2* pub2, float* theta, const int*
 // transposition into rank-major planes, per-qd occurrence / click counts, the
 // qd range of each query segment, and the click counts behind the public
 // constants (PBM: clicks per rank; UBM: written and clicked-written slots).
-__global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32_t* __restrict__ pidx_sm,
-                            const uint16_t* __restrict__ click, const int32_t* __restrict__ seg_id,
-                            int model, int32_t* planes, uint2* cnt, int* seg_lo, int* seg_hi,
-                            unsigned long long* pub_counts, uint32_t* packbits, int* flag) {
+//
+// Block b takes the contiguous sessions [b * chunk, (b + 1) * chunk) (chunk a
+// multiple of 32, so a warp's packbits word belongs to one block).  It first
+// finds the qd range of its sessions; when that range has at most kPrepHist
+// pairs -- always so inside a head query, whose sessions share one qd window --
+// the occurrence and click counts go into a shared histogram that is flushed
+// with one 64-bit atomic per pair.  Otherwise lanes with the same qd at a rank
+// add their counts with one global atomic.  (Global atomics alone put a head
+// query's few hot pairs on one L2 slice: 3.6 ms for 16M sessions.)
+constexpr int kPrepHist = 6144;  // uint2 entries: 48 KB of dynamic shared memory
+constexpr int kPrepThreads = 256;
+
+__global__ void __launch_bounds__(kPrepThreads) prep_kernel(
+    int64_t n, int64_t chunk, int64_t stride, int64_t n_qd, const int32_t* __restrict__ pidx_sm,
+    const uint16_t* __restrict__ click, const int32_t* __restrict__ seg_id, int model, int32_t* planes, uint2* cnt,
+    int* seg_lo, int* seg_hi, unsigned long long* pub_counts, uint32_t* packbits, int* flag) {
+    extern __shared__ uint2 hist[];
     __shared__ unsigned int sc[MC_PUB_COUNTS];
-    for (int k = threadIdx.x; k < MC_PUB_COUNTS; k += blockDim.x) sc[k] = 0;
+    __shared__ int s_lo, s_hi;
+    const int tid = threadIdx.x, lane = tid & 31;
+    for (int k = tid; k < MC_PUB_COUNTS; k += blockDim.x) sc[k] = 0;
+    if (tid == 0) { s_lo = INT_MAX; s_hi = INT_MIN; }
     __syncthreads();
-    const int64_t step = (int64_t)gridDim.x * blockDim.x;
-    const int64_t base = (int64_t)blockIdx.x * blockDim.x;
-    for (int64_t s0 = base; s0 < n; s0 += step) {
-        int64_t s = s0 + threadIdx.x;
-        bool valid = s < n;
+    const int64_t b0 = (int64_t)blockIdx.x * chunk;
+    const int64_t b1 = min(n, b0 + chunk);
+    {
+        int lo = INT_MAX, hi = INT_MIN;
+        for (int64_t s = b0 + tid; s < b1; s += blockDim.x) {
+#pragma unroll
+            for (int r = 0; r < MC_R; r++) {
+                const int p = pidx_sm[s * MC_R + r];
+                if (p >= 0 && (int64_t)p < n_qd) { lo = min(lo, p); hi = max(hi, p + 1); }
+            }
+        }
+        lo = __reduce_min_sync(0xffffffffu, lo);
+        hi = __reduce_max_sync(0xffffffffu, hi);
+        if (lane == 0) { atomicMin(&s_lo, lo); atomicMax(&s_hi, hi); }
+    }
+    __syncthreads();
+    const int h_lo = s_lo;
+    const int h_n = s_hi > s_lo ? s_hi - s_lo : 0;
+    const bool local = h_n <= kPrepHist;  // uniform over the block
+    if (local)
+        for (int k = tid; k < h_n; k += blockDim.x) hist[k] = make_uint2(0u, 0u);
+    __syncthreads();
+    for (int64_t s0 = b0; s0 < b1; s0 += blockDim.x) {
+        const int64_t s = s0 + tid;
+        const bool valid = s < b1;
         int lo = INT_MAX, hi = INT_MIN;
         int64_t seg = -1;
         const unsigned m = valid ? click[s] : 0u;
         // Bit s of packbits: session s has a click (32 consecutive sessions per warp).
         const unsigned word = __ballot_sync(0xffffffffu, m != 0u);
-        const int64_t w0 = s0 + (threadIdx.x & ~31);  // first session of this warp, a multiple of 32
-        if ((threadIdx.x & 31) == 0 && w0 < n) packbits[w0 >> 5] = word;
-        // The rank loop runs on every lane (invalid lanes hold p = -1) so that
-        // lanes with the same qd at a rank -- consecutive sessions of one
-        // query mostly -- add their occurrence and click counts with one
-        // 64-bit atomic ({occurrences, clicks} as the low and high word).
+        const int64_t w0 = s0 + (tid & ~31);  // first session of this warp, a multiple of 32
+        if (lane == 0 && w0 < b1) packbits[w0 >> 5] = word;
         if (valid) seg = seg_id[s];
         int last = 9, slot[MC_R];
 #pragma unroll
@@ -113,17 +154,25 @@ __global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32
                 hi = max(hi, p + 1);
             }
             const bool c = valid && ((m >> r) & 1u);
-            const unsigned peers = __match_any_sync(0xffffffffu, p);
-            const unsigned clicked = __ballot_sync(0xffffffffu, c) & peers;
-            if (valid && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
-                atomicAdd(reinterpret_cast<unsigned long long*>(cnt + p),
-                          (unsigned long long)__popc(peers) | ((unsigned long long)__popc(clicked) << 32));
-
+            if (local) {
+                const unsigned hp = (unsigned)(p - h_lo);
+                if (valid && hp < (unsigned)h_n) {
+                    atomicAdd(&hist[hp].x, 1u);
+                    if (c) atomicAdd(&hist[hp].y, 1u);
+                }
+            } else {
+                // every lane takes part in the match and the ballot (invalid lanes hold p = -1)
+                const unsigned peers = __match_any_sync(0xffffffffu, p);
+                const unsigned clicked = __ballot_sync(0xffffffffu, c) & peers;
+                if (valid && lane == __ffs(peers) - 1)
+                    atomicAdd(reinterpret_cast<unsigned long long*>(cnt + p),
+                              (unsigned long long)__popc(peers) | ((unsigned long long)__popc(clicked) << 32));
+            }
             slot[r] = r * (r + 1) / 2 + last;
             if (c) last = r;
             if (model == 0) {  // clicks per rank, summed over the warp
                 const unsigned nc = __popc(__ballot_sync(0xffffffffu, c));
-                if ((threadIdx.x & 31) == 0 && nc) atomicAdd(&sc[r], nc);
+                if (lane == 0 && nc) atomicAdd(&sc[r], nc);
             }
         }
         {  // per-session counts of the public constants, summed over the warp
@@ -132,34 +181,38 @@ __global__ void prep_kernel(int64_t n, int64_t stride, int64_t n_qd, const int32
             if (valid && model == 2) v = (unsigned)lc;
             if (valid && model == 1) v = (unsigned)(lc - __popc(m & ((1u << lc) - 1u)));
             v = __reduce_add_sync(0xffffffffu, v);
-            if ((threadIdx.x & 31) == 0 && v)
+            if (lane == 0 && v)
                 atomicAdd(&sc[model == 2 ? MC_CNT_DBN_BEFORE_LAST : MC_CNT_CCM_UNCLICKED_BEFORE_LAST], v);
         }
-        if (valid) {
-            if (model == 3) {
+        if (valid && model == 3) {
 #pragma unroll
-                for (int r = 0; r < MC_R; r++) {
-                    bool alive = true;
+            for (int r = 0; r < MC_R; r++) {
+                bool alive = true;
 #pragma unroll
-                    for (int r2 = r + 1; r2 < MC_R; r2++) alive = alive && slot[r2] != slot[r];
-                    if (alive) {
-                        atomicAdd(&sc[slot[r]], 1u);
-                        if ((m >> r) & 1u) atomicAdd(&sc[MC_UBM_SLOTS + slot[r]], 1u);
-                    }
+                for (int r2 = r + 1; r2 < MC_R; r2++) alive = alive && slot[r2] != slot[r];
+                if (alive) {
+                    atomicAdd(&sc[slot[r]], 1u);
+                    if ((m >> r) & 1u) atomicAdd(&sc[MC_UBM_SLOTS + slot[r]], 1u);
                 }
             }
         }
         // Segment ranges, aggregated over the lanes of a warp that share a segment.
-        unsigned peers = __match_any_sync(0xffffffffu, (unsigned long long)seg);
-        int wlo = __reduce_min_sync(peers, lo);
-        int whi = __reduce_max_sync(peers, hi);
-        if (valid && (threadIdx.x & 31) == __ffs(peers) - 1) {
+        const unsigned peers = __match_any_sync(0xffffffffu, (unsigned long long)seg);
+        const int wlo = __reduce_min_sync(peers, lo);
+        const int whi = __reduce_max_sync(peers, hi);
+        if (valid && lane == __ffs(peers) - 1) {
             atomicMin(&seg_lo[seg], wlo);
             atomicMax(&seg_hi[seg], whi);
         }
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < MC_PUB_COUNTS; k += blockDim.x)
+    if (local)
+        for (int k = tid; k < h_n; k += blockDim.x) {
+            const uint2 h = hist[k];
+            if (h.x) atomicAdd(reinterpret_cast<unsigned long long*>(cnt + h_lo + k),
+                               (unsigned long long)h.x | ((unsigned long long)h.y << 32));
+        }
+    for (int k = tid; k < MC_PUB_COUNTS; k += blockDim.x)
         if (sc[k]) atomicAdd(&pub_counts[k], (unsigned long long)sc[k]);
 }
 
@@ -281,6 +334,7 @@ struct mc_model {
     SplitDev* d_splits = nullptr;
     WorkState* d_ws = nullptr;
     int n_tiles = 0, n_splits = 0, grid = 0;
+    bool tiles_ready = false;  // tiles built for the current shape (PBM/UBM build them only for batches)
     unsigned char* d_tblk = nullptr;
     int64_t split_bins_count = 0;
     int64_t tile_bytes = 0;
@@ -321,6 +375,7 @@ struct mc_model {
     }
 
     void free_tiles() {
+        settle(d_tiles, d_splits, d_split_bins, d_split_count, d_tblk);
         dfree(d_tiles);
         dfree(d_splits);
         dfree(d_split_bins);
@@ -328,9 +383,11 @@ struct mc_model {
         dfree(d_tblk);
         bytes -= tile_bytes;
         tile_bytes = 0;
+        tiles_ready = false;
     }
 
     void free_plain() {
+        settle(d_recs, d_atr2, d_sat2, d_pub2, d_tmp_atr, d_tmp_sat, d_tmp_pub);
         dfree(d_recs); dfree(d_atr2); dfree(d_sat2); dfree(d_pub2); dfree(d_tmp_atr); dfree(d_tmp_sat); dfree(d_tmp_pub);
         bytes -= plain_bytes;
         plain_bytes = 0;
@@ -340,6 +397,7 @@ struct mc_model {
         drop_graph();
         free_tiles();
         free_plain();
+        settle(d_pidx, d_click, d_atr, d_fit, d_grad);
         dfree(d_pidx); dfree(d_click); dfree(d_cnt); dfree(d_cnt16); dfree(d_coff); dfree(d_cent); dfree(d_atr); dfree(d_sat); dfree(d_pub_theta);
         dfree(d_pub_bins); dfree(d_pub_const); dfree(d_tiles_done); dfree(d_iter); dfree(d_status);
         dfree(d_fit); dfree(d_ws); dfree(d_grad);
@@ -349,6 +407,7 @@ struct mc_model {
     }
 
     void free_test() {
+        settle(d_test_pidx, d_test_click, d_eval);
         dfree(d_test_pidx); dfree(d_test_click); dfree(d_eval);
         bytes -= test_bytes;
         test_bytes = 0;
@@ -363,6 +422,12 @@ struct mc_model {
 
     int64_t qd_alloc() const { return ((std::max<int64_t>(n_qd, 1) + 3) & ~(int64_t)3) + 4; }
     int build_tiles();
+    // Tiles for the tile kernel (batched launches, autotuning): built at upload
+    // for DBN/CCM, on first use for the count-path models.
+    int ensure_tiles() {
+        if (!fused_ok) return set_error(MC_ERR_INVALID, "tile path unavailable: " + fused_reason);
+        return tiles_ready ? MC_OK : build_tiles();
+    }
     FitDev make_desc() const;
     int write_fit_desc();
     int ensure_plain(cudaStream_t st);
@@ -584,6 +649,7 @@ int mc_model::build_tiles() {
     int status = 0;
     CK(cudaMemcpy(&status, d_status, 4, cudaMemcpyDeviceToHost));
     if (status) return set_error(MC_ERR_INVALID, "tile packing found a parameter index outside its query's window");
+    tiles_ready = true;
     return MC_OK;
 }
 
@@ -781,9 +847,14 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     ck(cudaMemsetAsync(m->d_pidx, 0, (size_t)(m->stride * MC_R) * 4, st));
     ck(cudaMemsetAsync(m->d_cnt, 0, (size_t)qd_alloc * sizeof(uint2), st));
     if (n && e == cudaSuccess) {
-        int grid = (int)std::min<int64_t>((n + 255) / 256, (int64_t)8 * m->n_sm);
-        prep_kernel<<<grid, 256, 0, st>>>(n, m->stride, n_qd, d_src, m->d_click, d_seg_id, m->model,
-                                          m->d_pidx, m->d_cnt, d_seg_lo, d_seg_hi, d_pub_counts, d_packbits, d_flag);
+        const int64_t grid = std::min<int64_t>((n + kPrepThreads - 1) / kPrepThreads, (int64_t)4 * m->n_sm);
+        const int64_t chunk = ((n + grid - 1) / grid + 31) / 32 * 32;
+        const int blocks = (int)((n + chunk - 1) / chunk);
+        const int hist_bytes = kPrepHist * (int)sizeof(uint2);
+        ck(cudaFuncSetAttribute(prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, hist_bytes));
+        prep_kernel<<<blocks, kPrepThreads, hist_bytes, st>>>(n, chunk, m->stride, n_qd, d_src, m->d_click, d_seg_id,
+                                                              m->model, m->d_pidx, m->d_cnt, d_seg_lo, d_seg_hi,
+                                                              d_pub_counts, d_packbits, d_flag);
         ck(cudaGetLastError());
     }
     {
@@ -874,7 +945,7 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     // The count path (PBM/UBM) reads the fit descriptor whether or not the
     // sessions admit tiles; build_tiles rewrites it with the tile fields.
     if ((rc = m->write_fit_desc())) return rc;
-    if (m->fused_ok && (rc = m->build_tiles())) return rc;
+    if (m->fused_ok && !m->d_coff && (rc = m->build_tiles())) return rc;
     return MC_OK;
 }
 
@@ -917,7 +988,8 @@ extern "C" int mc_model_configure(mc_model* m, int32_t spt, int32_t wqd, int32_t
     if (block) m->block = block;
     // Unchanged shape: the tiles, occupancy and graphs stay valid.
     if (m->spt == spt0 && m->wqd == wqd0 && m->block == block0) return MC_OK;
-    if (m->uploaded && m->fused_ok) return m->build_tiles();
+    // Count-path models rebuild tiles only if a batch already made them.
+    if (m->uploaded && m->fused_ok && (!m->d_coff || m->tiles_ready)) return m->build_tiles();
     return MC_OK;
 }
 
@@ -1189,7 +1261,9 @@ extern "C" int mc_model_em_trace(mc_model* m, int32_t iters, double* train_ll, v
 
 extern "C" int mc_model_autotune(mc_model* m, void* stream) {
     if (!m) return set_error(MC_ERR_INVALID, "autotune: null model");
-    if (!m->uploaded || !m->fused_ok) return set_error(MC_ERR_STATE, "autotune: needs uploaded sessions and the fused path");
+    if (!m->uploaded || (!m->fused_ok && !m->d_coff))
+        return set_error(MC_ERR_STATE, "autotune: needs uploaded sessions and the fused path");
+    if (m->d_coff) return MC_OK;  // the count kernel has no tile shape to tune
     CK(cudaSetDevice(m->device));
     cudaStream_t st = m->pick(stream);
     CK(cudaStreamSynchronize(st));
@@ -1286,6 +1360,7 @@ struct mc_batch {
 
     void release() {
         for (auto& g : graphs) { if (g.exec) cudaGraphExecDestroy(g.exec); g.exec = nullptr; g.iters = -1; }
+        settle(d_fits, d_tiles, d_splits, d_ws);
         dfree(d_fits); dfree(d_tiles); dfree(d_splits); dfree(d_ws);
         if (own_stream) cudaStreamDestroy(own_stream);
         own_stream = nullptr;
@@ -1333,6 +1408,7 @@ extern "C" int mc_batch_create(int n_models, mc_model* const* models, mc_batch**
     for (int i = 0; i < n_models; i++) {
         mc_model* m = models[i];
         if (m->model != b->kernel_model) b->kernel_model = -1;
+        if (int rc = m->ensure_tiles()) { delete b; return rc; }
         fits.push_back(m->make_desc());
         std::vector<TileDev> t((size_t)m->n_tiles);
         std::vector<SplitDev> sp((size_t)m->n_splits);
