@@ -82,12 +82,17 @@ __global__ void pairs_to_pub_kernel(const float2* pub2, float* theta, const int*
     }
 }
 
+__global__ void fill_i32_kernel(int* __restrict__ p, int64_t n, int v) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
 // One pass over the uploaded sessions (session-major pidx): range check,
 // transposition into rank-major planes, per-qd occurrence / click counts, the
 // qd range of each query segment, and the click counts behind the public
 // constants (PBM: clicks per rank; UBM: written and clicked-written slots).
 //
-// Block b takes the contiguous sessions [b * chunk, (b + 1) * chunk) (chunk a
+// One launch covers the sessions [s_first, s_end) (s_first a multiple of 32);
+// block b takes the contiguous sessions from s_first + b * chunk (chunk a
 // multiple of 32, so a warp's packbits word belongs to one block).  It first
 // finds the qd range of its sessions; when that range has at most kPrepHist
 // pairs -- always so inside a head query, whose sessions share one qd window --
@@ -99,7 +104,7 @@ constexpr int kPrepHist = 6144;  // uint2 entries: 48 KB of dynamic shared memor
 constexpr int kPrepThreads = 256;
 
 __global__ void __launch_bounds__(kPrepThreads) prep_kernel(
-    int64_t n, int64_t chunk, int64_t stride, int64_t n_qd, const int32_t* __restrict__ pidx_sm,
+    int64_t s_first, int64_t s_end, int64_t chunk, int64_t stride, int64_t n_qd, const int32_t* __restrict__ pidx_sm,
     const uint16_t* __restrict__ click, const int32_t* __restrict__ seg_id, int model, int32_t* planes, uint2* cnt,
     int* seg_lo, int* seg_hi, unsigned long long* pub_counts, uint32_t* packbits, int* flag) {
     extern __shared__ uint2 hist[];
@@ -109,8 +114,8 @@ __global__ void __launch_bounds__(kPrepThreads) prep_kernel(
     for (int k = tid; k < MC_PUB_COUNTS; k += blockDim.x) sc[k] = 0;
     if (tid == 0) { s_lo = INT_MAX; s_hi = INT_MIN; }
     __syncthreads();
-    const int64_t b0 = (int64_t)blockIdx.x * chunk;
-    const int64_t b1 = min(n, b0 + chunk);
+    const int64_t b0 = s_first + (int64_t)blockIdx.x * chunk;
+    const int64_t b1 = min(s_end, b0 + chunk);
     {
         int lo = INT_MAX, hi = INT_MIN;
         for (int64_t s = b0 + tid; s < b1; s += blockDim.x) {
@@ -308,13 +313,18 @@ struct ParamDesc {
 
 }  // namespace
 
+// Chunks of the upload's host-to-device copy of the session indices; the
+// upload pass runs on each chunk as soon as it has landed.
+static const int kUploadChunks = 8;
+
 struct mc_model {
     int model = 0, mode = 0, device = 0, n_pub = 0, n_sm = 0;
     int64_t n = 0, stride = 0, n_qd = 0, bytes = 0;
     bool uploaded = false, fused_ok = false;
     std::string fused_reason;
     // query segments of the training set: sessions and qd range
-    std::vector<int64_t> seg_begin, seg_lo, seg_hi;
+    std::vector<int64_t> seg_begin;
+    std::vector<int32_t> seg_lo, seg_hi;  // qd range [lo, hi) of each segment, as the upload pass finds it
     std::vector<uint32_t> packbits;  // bit s: training session s has a click
     int spt = 1024, wqd = 1536, block = 256, stages = 2, ctas_per_sm = 1;
     // fused state
@@ -356,6 +366,16 @@ struct mc_model {
     struct GraphSlot { cudaGraphExec_t exec = nullptr; int iters = -1; };  // also used by mc_batch
     GraphSlot graphs[2];
     cudaStream_t own_stream = nullptr;
+    // Side stream of the upload's host-to-device copies and one event per chunk.
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_ev[kUploadChunks + 1] = {};
+
+    int ensure_copy_stream() {
+        if (!copy_stream) CK(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+        for (cudaEvent_t& ev : copy_ev)
+            if (!ev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        return MC_OK;
+    }
 
     std::vector<ParamDesc> params() const {
         switch (model) {
@@ -748,6 +768,46 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     m->n_qd = n_qd;
     m->stride = std::max<int64_t>(32, (n + 31) / 32 * 32);
 
+    // The session indices and clicks go up on a side stream, in chunks, while
+    // the query segments are found on st; the upload pass then runs on each
+    // chunk as its copy lands.  The side stream first waits for the work
+    // already queued on st (which may still be writing the host buffers).
+    int rc;
+    int32_t* d_src = nullptr;
+    int64_t scratch = 0;
+    if ((rc = dalloc(&d_src, (size_t)std::max<int64_t>(n * MC_R, 1), &scratch))) return rc;
+    if ((rc = dalloc(&m->d_click, (size_t)std::max<int64_t>(n, 1), &m->bytes))) { dfree(d_src); return rc; }
+    int n_chunks = 0;
+    int64_t chunk_at[kUploadChunks + 1] = {0};
+    if (n) {
+        cudaError_t ec = cudaSuccess;
+        if ((rc = m->ensure_copy_stream())) { dfree(d_src); return rc; }
+        cudaStream_t cs = m->copy_stream;
+        n_chunks = (int)std::min<int64_t>(kUploadChunks, std::max<int64_t>(1, n / 65536));
+        for (int k = 0; k < n_chunks; k++) chunk_at[k] = std::min<int64_t>(n, (n * k / n_chunks + 31) / 32 * 32);
+        chunk_at[n_chunks] = n;
+        if (ec == cudaSuccess) ec = cudaEventRecord(m->copy_ev[kUploadChunks], st);
+        if (ec == cudaSuccess) ec = cudaStreamWaitEvent(cs, m->copy_ev[kUploadChunks], 0);
+        if (ec == cudaSuccess) ec = cudaMemcpyAsync(m->d_click, click, (size_t)n * 2, cudaMemcpyHostToDevice, cs);
+        for (int k = 0; k < n_chunks && ec == cudaSuccess; k++) {
+            const int64_t c0 = chunk_at[k], c1 = chunk_at[k + 1];
+            if (c1 > c0)
+                ec = cudaMemcpyAsync(d_src + c0 * MC_R, pidx + c0 * MC_R, (size_t)(c1 - c0) * MC_R * 4, cudaMemcpyHostToDevice, cs);
+            if (ec == cudaSuccess) ec = cudaEventRecord(m->copy_ev[k], cs);
+        }
+        if (ec != cudaSuccess) {
+            cudaStreamSynchronize(cs);
+            dfree(d_src);
+            m->free_train();
+            return cuda_fail("model_upload", ec);
+        }
+    }
+    // Frees the scratch after the copies and st have drained.
+    auto drain = [&]() {
+        if (m->copy_stream) cudaStreamSynchronize(m->copy_stream);
+        cudaStreamSynchronize(st);
+    };
+
     // Query segments (runs of equal query id), found on the device: block
     // counts, their prefix on the host, then seg_begin and each session's
     // segment index.
@@ -766,7 +826,8 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
             (rc0 = dalloc(&d_seg_id, (size_t)std::max<int64_t>(n, 1), &scratch0)) ||
             (rc0 = dalloc(&d_blk, (size_t)std::max<int64_t>(nb, 1), &scratch0)) ||
             (rc0 = dalloc(&d_off, (size_t)std::max<int64_t>(nb, 1), &scratch0))) {
-            free0(); dfree(d_q); dfree(d_seg_id);
+            drain();
+            free0(); dfree(d_q); dfree(d_seg_id); dfree(d_src);
             return rc0;
         }
         std::vector<int> blk((size_t)nb);
@@ -781,7 +842,8 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
             ck0(cudaStreamSynchronize(st));
             for (int64_t b = 0; b < nb; b++) { off[(size_t)b] = n_seg; n_seg += blk[(size_t)b]; }
             if (e0 == cudaSuccess && (rc0 = dalloc(&d_seg_begin, (size_t)std::max<int64_t>(n_seg, 1), &scratch0))) {
-                free0(); dfree(d_q); dfree(d_seg_id);
+                drain();
+                free0(); dfree(d_q); dfree(d_seg_id); dfree(d_src);
                 return rc0;
             }
             ck0(cudaMemcpyAsync(d_off, off.data(), (size_t)nb * 8, cudaMemcpyHostToDevice, st));
@@ -793,14 +855,20 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
         ck0(cudaStreamSynchronize(st));
         free0();
         dfree(d_q);
-        if (e0 != cudaSuccess) { dfree(d_seg_id); dfree(d_seg_begin); return cuda_fail("model_upload", e0); }
+        if (e0 != cudaSuccess) {
+            drain();
+            dfree(d_seg_id); dfree(d_seg_begin); dfree(d_src);
+            return cuda_fail("model_upload", e0);
+        }
     }
 
-    int rc;
     int64_t& B = m->bytes;
-    auto fail_seg = [&](int code) { dfree(d_seg_id); dfree(d_seg_begin); return code; };
+    auto fail_seg = [&](int code) {
+        drain();
+        dfree(d_seg_id); dfree(d_seg_begin); dfree(d_src);
+        return code;
+    };
     if ((rc = dalloc(&m->d_pidx, (size_t)(m->stride * MC_R), &B))) return fail_seg(rc);
-    if ((rc = dalloc(&m->d_click, (size_t)std::max<int64_t>(n, 1), &B))) return fail_seg(rc);
     // Parameter arrays padded to a multiple of 4 entries plus 4, so 16-byte
     // aligned bulk copies of any window stay inside the allocation.
     const int64_t qd_alloc = m->qd_alloc();
@@ -818,44 +886,49 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     if ((rc = dalloc(&m->d_ws, 1, &B))) return fail_seg(rc);
 
     // Scratch for the preparation pass.
-    int32_t* d_src = nullptr;
     int *d_seg_lo = nullptr, *d_seg_hi = nullptr, *d_flag = nullptr;
     unsigned long long* d_pub_counts = nullptr;
     uint32_t* d_packbits = nullptr;
     const int64_t n_words = (n + 31) / 32;
-    int64_t scratch = 0;
-    auto free_scratch = [&]() { dfree(d_src); dfree(d_seg_begin); dfree(d_seg_id); dfree(d_seg_lo); dfree(d_seg_hi); dfree(d_flag); dfree(d_pub_counts); dfree(d_packbits); };
-    if ((rc = dalloc(&d_src, (size_t)std::max<int64_t>(n * MC_R, 1), &scratch)) ||
-        (rc = dalloc(&d_seg_lo, (size_t)std::max<int64_t>(n_seg, 1), &scratch)) ||
+    auto free_scratch = [&]() { drain(); dfree(d_src); dfree(d_seg_begin); dfree(d_seg_id); dfree(d_seg_lo); dfree(d_seg_hi); dfree(d_flag); dfree(d_pub_counts); dfree(d_packbits); };
+    if ((rc = dalloc(&d_seg_lo, (size_t)std::max<int64_t>(n_seg, 1), &scratch)) ||
         (rc = dalloc(&d_seg_hi, (size_t)std::max<int64_t>(n_seg, 1), &scratch)) ||
         (rc = dalloc(&d_flag, 1, &scratch)) || (rc = dalloc(&d_pub_counts, MC_PUB_COUNTS, &scratch)) ||
         (rc = dalloc(&d_packbits, (size_t)std::max<int64_t>(n_words, 1), &scratch))) {
         free_scratch();
         return rc;
     }
-    std::vector<int> init_lo((size_t)std::max<int64_t>(n_seg, 1), INT_MAX), init_hi((size_t)std::max<int64_t>(n_seg, 1), INT_MIN);
     cudaError_t e = cudaSuccess;
     auto ck = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-    if (n) {
-        ck(cudaMemcpyAsync(d_src, pidx, (size_t)n * MC_R * 4, cudaMemcpyHostToDevice, st));
-        ck(cudaMemcpyAsync(m->d_click, click, (size_t)n * 2, cudaMemcpyHostToDevice, st));
+    {
+        const int64_t ns = std::max<int64_t>(n_seg, 1);
+        const int g = (int)std::min<int64_t>((ns + 255) / 256, (int64_t)4 * m->n_sm);
+        fill_i32_kernel<<<g, 256, 0, st>>>(d_seg_lo, ns, INT_MAX);
+        fill_i32_kernel<<<g, 256, 0, st>>>(d_seg_hi, ns, INT_MIN);
+        ck(cudaGetLastError());
     }
-    ck(cudaMemcpyAsync(d_seg_lo, init_lo.data(), init_lo.size() * 4, cudaMemcpyHostToDevice, st));
-    ck(cudaMemcpyAsync(d_seg_hi, init_hi.data(), init_hi.size() * 4, cudaMemcpyHostToDevice, st));
     ck(cudaMemsetAsync(d_flag, 0, 4, st));
     ck(cudaMemsetAsync(d_pub_counts, 0, MC_PUB_COUNTS * 8, st));
-    ck(cudaMemsetAsync(m->d_pidx, 0, (size_t)(m->stride * MC_R) * 4, st));
+    // Planes: the upload pass writes sessions [0, n); only the padding up to
+    // the stride needs clearing.
+    if (m->stride > n)
+        ck(cudaMemset2DAsync(m->d_pidx + n, (size_t)m->stride * 4, 0, (size_t)(m->stride - n) * 4, MC_R, st));
     ck(cudaMemsetAsync(m->d_cnt, 0, (size_t)qd_alloc * sizeof(uint2), st));
     if (n && e == cudaSuccess) {
-        const int64_t grid = std::min<int64_t>((n + kPrepThreads - 1) / kPrepThreads, (int64_t)4 * m->n_sm);
-        const int64_t chunk = ((n + grid - 1) / grid + 31) / 32 * 32;
-        const int blocks = (int)((n + chunk - 1) / chunk);
         const int hist_bytes = kPrepHist * (int)sizeof(uint2);
         ck(cudaFuncSetAttribute(prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, hist_bytes));
-        prep_kernel<<<blocks, kPrepThreads, hist_bytes, st>>>(n, chunk, m->stride, n_qd, d_src, m->d_click, d_seg_id,
-                                                              m->model, m->d_pidx, m->d_cnt, d_seg_lo, d_seg_hi,
-                                                              d_pub_counts, d_packbits, d_flag);
-        ck(cudaGetLastError());
+        for (int k = 0; k < n_chunks && e == cudaSuccess; k++) {
+            const int64_t c0 = chunk_at[k], c1 = chunk_at[k + 1], len = c1 - c0;
+            ck(cudaStreamWaitEvent(st, m->copy_ev[k], 0));
+            if (len <= 0) continue;
+            const int64_t grid = std::min<int64_t>((len + kPrepThreads - 1) / kPrepThreads, (int64_t)4 * m->n_sm);
+            const int64_t chunk = ((len + grid - 1) / grid + 31) / 32 * 32;
+            const int blocks = (int)((len + chunk - 1) / chunk);
+            prep_kernel<<<blocks, kPrepThreads, hist_bytes, st>>>(c0, c1, chunk, m->stride, n_qd, d_src, m->d_click,
+                                                                  d_seg_id, m->model, m->d_pidx, m->d_cnt, d_seg_lo,
+                                                                  d_seg_hi, d_pub_counts, d_packbits, d_flag);
+            ck(cudaGetLastError());
+        }
     }
     {
         int grid = (int)std::min<int64_t>((qd_alloc + 255) / 256, (int64_t)8 * m->n_sm);
@@ -864,13 +937,16 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     }
     int flag = 0;
     std::vector<unsigned long long> pub_counts(MC_PUB_COUNTS, 0);
-    std::vector<int> lo(init_lo.size()), hi(init_hi.size());
     ck(cudaMemcpyAsync(&flag, d_flag, 4, cudaMemcpyDeviceToHost, st));
     ck(cudaMemcpyAsync(pub_counts.data(), d_pub_counts, pub_counts.size() * 8, cudaMemcpyDeviceToHost, st));
     m->packbits.assign((size_t)n_words, 0u);
     if (n_words) ck(cudaMemcpyAsync(m->packbits.data(), d_packbits, (size_t)n_words * 4, cudaMemcpyDeviceToHost, st));
-    ck(cudaMemcpyAsync(lo.data(), d_seg_lo, lo.size() * 4, cudaMemcpyDeviceToHost, st));
-    ck(cudaMemcpyAsync(hi.data(), d_seg_hi, hi.size() * 4, cudaMemcpyDeviceToHost, st));
+    m->seg_lo.resize((size_t)n_seg);
+    m->seg_hi.resize((size_t)n_seg);
+    if (n_seg) {
+        ck(cudaMemcpyAsync(m->seg_lo.data(), d_seg_lo, (size_t)n_seg * 4, cudaMemcpyDeviceToHost, st));
+        ck(cudaMemcpyAsync(m->seg_hi.data(), d_seg_hi, (size_t)n_seg * 4, cudaMemcpyDeviceToHost, st));
+    }
     ck(cudaStreamSynchronize(st));
     free_scratch();
     if (e != cudaSuccess) return cuda_fail("model_upload", e);
@@ -894,8 +970,6 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     }
 
     // Fused path precondition: per-query qd ranges disjoint and increasing.
-    m->seg_lo.assign(lo.begin(), lo.begin() + n_seg);
-    m->seg_hi.assign(hi.begin(), hi.begin() + n_seg);
     m->fused_ok = true;
     for (int64_t g = 1; g < n_seg; g++)
         if (m->seg_lo[(size_t)g] < m->seg_hi[(size_t)g - 1]) {
@@ -1326,6 +1400,9 @@ extern "C" void mc_model_destroy(mc_model* m) {
     m->free_test();
     m->free_train();
     if (m->own_stream) cudaStreamDestroy(m->own_stream);
+    if (m->copy_stream) cudaStreamDestroy(m->copy_stream);
+    for (cudaEvent_t ev : m->copy_ev)
+        if (ev) cudaEventDestroy(ev);
     delete m;
 }
 
