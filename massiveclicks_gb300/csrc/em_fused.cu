@@ -55,6 +55,7 @@
 //     is needed until the final ratio.
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <cub/block/block_radix_sort.cuh>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -972,44 +973,66 @@ cudaError_t fused_occupancy(int model, int block, size_t smem, int* blocks_per_s
 // uint16 window-relative indices [10][spad] followed by the click masks
 // [spad] (padding zeroed), spad = s_packed rounded up to 8.  Sessions are
 // ordered by click pattern (DBN/CCM: last-click rank, then mask; PBM/UBM:
-// click mask), a
-// stable bitonic sort on (key, position), so the lanes of a warp take the
-// same branches.  DBN and CCM sessions without clicks carry no variable
-// statistic (their constant contributions are folded in at upload) and are
-// left out; s_packed records how many sessions remain.  Direct tiles keep no
-// packed block.
-__global__ void pack_tiles_kernel(int model, TileDev* tiles, int n_tiles, int window_max, const int32_t* planes,
-                                  int64_t stride, const uint16_t* click, unsigned char* tblk, int* status) {
+// click mask) so the lanes of a warp take the same branches: a block radix
+// sort of (pattern << 16 | position) on the 14 pattern bits, stable, so equal
+// patterns keep their session order.  DBN and CCM sessions without clicks
+// carry no variable statistic (their constant contributions are folded in at
+// upload) and are left out; s_packed records how many sessions remain.
+// Direct tiles keep no packed block.
+constexpr int kPackThreads = 256;
+constexpr int kPackMinKeys = 4 * kPackThreads;  // keys[] holds at least this many
+
+template <int ITEMS>
+using PackSort = cub::BlockRadixSort<uint32_t, kPackThreads, ITEMS, cub::NullType, 5>;
+
+union PackSortStorage {
+    typename PackSort<4>::TempStorage s4;
+    typename PackSort<8>::TempStorage s8;
+    typename PackSort<16>::TempStorage s16;
+};
+
+// Sort keys of one tile's sessions, in blocked order (thread t holds
+// positions t * ITEMS ...): pattern in the high half, position in the low;
+// positions past the tile get the largest key.  Sorted keys go to keys[].
+template <int ITEMS>
+__device__ __forceinline__ void pack_sort(PackSortStorage& tmp, uint32_t* keys, const uint16_t* click, int64_t s_begin,
+                                          int s_count, bool drop_clickless) {
+    uint32_t k[ITEMS];
+#pragma unroll
+    for (int j = 0; j < ITEMS; j++) {
+        const int i = threadIdx.x * ITEMS + j;
+        uint32_t key = 0xFFFFFFFFu;
+        if (i < s_count) {
+            const unsigned m = click[s_begin + i];
+            const uint32_t k16 = drop_clickless ? (m ? (((uint32_t)(31 - __clz(m)) << 10) | m) : 0xFFFFu) : m;
+            key = (k16 << 16) | (uint32_t)i;
+        }
+        k[j] = key;
+    }
+    // Patterns are below 0x2800; clickless sessions and padding (0xFFFF) read
+    // 0x3FFF on bits [16, 30) and sort after them, padding last (stability).
+    PackSort<ITEMS>(reinterpret_cast<typename PackSort<ITEMS>::TempStorage&>(tmp)).Sort(k, 16, 30);
+#pragma unroll
+    for (int j = 0; j < ITEMS; j++) keys[threadIdx.x * ITEMS + j] = k[j];
+}
+
+__global__ void __launch_bounds__(kPackThreads) pack_tiles_kernel(int model, TileDev* tiles, int n_tiles, int window_max,
+                                                                 const int32_t* planes, int64_t stride,
+                                                                 const uint16_t* click, unsigned char* tblk, int* status) {
     extern __shared__ uint32_t keys[];
+    __shared__ PackSortStorage sort_tmp;
     __shared__ int s_kept;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
         const TileDev tile = tiles[t];
         if (tile.qd_count > window_max) continue;
         const bool drop_clickless = model == DBN || model == CCM;
-        int P = 1;
-        while (P < tile.s_count) P <<= 1;
-        for (int i = threadIdx.x; i < P; i += blockDim.x) {
-            uint32_t key = 0xFFFFFFFFu;
-            if (i < tile.s_count) {
-                unsigned m = click[tile.s_begin + i];
-                uint32_t k16 = drop_clickless ? (m ? (((uint32_t)(31 - __clz(m)) << 10) | m) : 0xFFFFu) : m;
-                key = (k16 << 16) | (uint32_t)i;
-            }
-            keys[i] = key;
-        }
+        if (tile.s_count <= 4 * kPackThreads)
+            pack_sort<4>(sort_tmp, keys, click, tile.s_begin, tile.s_count, drop_clickless);
+        else if (tile.s_count <= 8 * kPackThreads)
+            pack_sort<8>(sort_tmp, keys, click, tile.s_begin, tile.s_count, drop_clickless);
+        else
+            pack_sort<16>(sort_tmp, keys, click, tile.s_begin, tile.s_count, drop_clickless);
         __syncthreads();
-        for (int k = 2; k <= P; k <<= 1)
-            for (int j = k >> 1; j > 0; j >>= 1) {
-                for (int i = threadIdx.x; i < P; i += blockDim.x) {
-                    int ixj = i ^ j;
-                    if (ixj > i) {
-                        uint32_t x = keys[i], y = keys[ixj];
-                        bool up = (i & k) == 0;
-                        if ((x > y) == up) { keys[i] = y; keys[ixj] = x; }
-                    }
-                }
-                __syncthreads();
-            }
         int kept = 0;
         for (int i = threadIdx.x; i < tile.s_count; i += blockDim.x) kept += (keys[i] >> 16) != 0xFFFFu;
         if (threadIdx.x == 0) s_kept = 0;
@@ -1044,10 +1067,12 @@ cudaError_t launch_pack_tiles(int model, TileDev* tiles, int n_tiles, int window
                               int64_t stride, const uint16_t* click, unsigned char* tblk, int* status, int n_sm,
                               cudaStream_t st) {
     if (n_tiles == 0) return cudaSuccess;
-    int P = 1;
+    // keys[] holds 256 x ITEMS keys of the largest class a tile may take.
+    int P = kPackMinKeys;
     while (P < max_tile_sessions) P <<= 1;
     int g = n_tiles < 8 * n_sm ? n_tiles : 8 * n_sm;
-    pack_tiles_kernel<<<g, 256, (size_t)P * 4, st>>>(model, tiles, n_tiles, window_max, planes, stride, click, tblk, status);
+    pack_tiles_kernel<<<g, kPackThreads, (size_t)P * 4, st>>>(model, tiles, n_tiles, window_max, planes, stride, click,
+                                                              tblk, status);
     return cudaGetLastError();
 }
 

@@ -25,6 +25,7 @@
 #include "mclicks.h"
 #include "host_internal.h"
 #include "devmem.h"
+#include "pool.h"
 #include "common.cuh"
 #include "kernels.h"
 
@@ -80,6 +81,12 @@ __global__ void pairs_to_pub_kernel(const float2* pub2, float* theta, const int*
         float v = pub2[k].x / pub2[k].y;
         theta[(*iter & 1) * MC_MAX_PUB + k] = v < MC_TOP ? v : MC_TOP;
     }
+}
+
+// flag = 1 when some query segment's qd range starts below the previous one's end.
+__global__ void seg_order_kernel(int64_t n_seg, const int* __restrict__ lo, const int* __restrict__ hi, int* flag) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x + 1; g < n_seg; g += (int64_t)gridDim.x * blockDim.x)
+        if (lo[g] < hi[g - 1]) *flag = 1;
 }
 
 __global__ void fill_i32_kernel(int* __restrict__ p, int64_t n, int v) {
@@ -485,9 +492,12 @@ int mc_model::build_tiles() {
     };
     const int64_t max_sess = std::max<int64_t>(spt, kTileSessions);
     const size_t n_seg = seg_lo.size();
-    // Segments are tiled in fixed chunks of 65536 on several host threads (a
-    // chunk boundary also ends a tile, wherever the threads run); the chunks'
-    // tile and split lists are then joined in order.
+    // Segments are tiled in chunks on several host threads (a chunk boundary
+    // also ends a tile, wherever the threads run); the chunks' tile and split
+    // lists are then joined in order.  A chunk's work grows with its segments
+    // and with its sessions (popcounts over their click words), and a head
+    // query holds millions of sessions, so chunks are cut at equal shares of
+    // segments + sessions / 32.
     auto build_range = [&](size_t g0, size_t g1, std::vector<TileDev>& tiles, std::vector<SplitDev>& splits,
                            int64_t& bin_off) {
         TileDev cur{};
@@ -581,23 +591,30 @@ int mc_model::build_tiles() {
         }
         close();
     };
-    const size_t kChunk = 65536;
-    const size_t n_chunks = (n_seg + kChunk - 1) / kChunk;
+    const size_t n_threads = mch::pool_threads();
+    // Work before segment g, g + seg_begin[g] / 32, grows with g: each cut is
+    // a binary search for the next share.
+    std::vector<size_t> cut{0};
+    {
+        auto work = [&](size_t g) { return (int64_t)g + seg_begin[g] / 32; };
+        const int64_t per = std::max<int64_t>(4096, work(n_seg) / (int64_t)(4 * n_threads) + 1);
+        while (cut.back() < n_seg) {
+            const int64_t target = work(cut.back()) + per;
+            size_t lo = cut.back() + 1, hi = n_seg;  // first g in [lo, hi] with work(g) >= target, else n_seg
+            while (lo < hi) {
+                const size_t mid = lo + (hi - lo) / 2;
+                if (work(mid) >= target) hi = mid; else lo = mid + 1;
+            }
+            cut.push_back(lo);
+        }
+    }
+    const size_t n_chunks = n_seg ? cut.size() - 1 : 0;
     std::vector<std::vector<TileDev>> chunk_tiles(n_chunks);
     std::vector<std::vector<SplitDev>> chunk_splits(n_chunks);
     std::vector<int64_t> chunk_bins(n_chunks, 0);
-    {
-        std::atomic<size_t> next{0};
-        auto worker = [&]() {
-            for (size_t c; (c = next.fetch_add(1)) < n_chunks;)
-                build_range(c * kChunk, std::min(n_seg, (c + 1) * kChunk), chunk_tiles[c], chunk_splits[c], chunk_bins[c]);
-        };
-        const size_t nth = std::max<size_t>(1, std::min<size_t>(std::thread::hardware_concurrency(), n_chunks));
-        std::vector<std::thread> pool;
-        for (size_t t = 1; t < nth; t++) pool.emplace_back(worker);
-        worker();
-        for (auto& th : pool) th.join();
-    }
+    mch::parallel_for(n_chunks, [&](size_t c) {
+        build_range(cut[c], cut[c + 1], chunk_tiles[c], chunk_splits[c], chunk_bins[c]);
+    });
     std::vector<TileDev> tiles;
     std::vector<SplitDev> splits;
     int64_t bin_off = 0;
@@ -893,7 +910,7 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     auto free_scratch = [&]() { drain(); dfree(d_src); dfree(d_seg_begin); dfree(d_seg_id); dfree(d_seg_lo); dfree(d_seg_hi); dfree(d_flag); dfree(d_pub_counts); dfree(d_packbits); };
     if ((rc = dalloc(&d_seg_lo, (size_t)std::max<int64_t>(n_seg, 1), &scratch)) ||
         (rc = dalloc(&d_seg_hi, (size_t)std::max<int64_t>(n_seg, 1), &scratch)) ||
-        (rc = dalloc(&d_flag, 1, &scratch)) || (rc = dalloc(&d_pub_counts, MC_PUB_COUNTS, &scratch)) ||
+        (rc = dalloc(&d_flag, 2, &scratch)) || (rc = dalloc(&d_pub_counts, MC_PUB_COUNTS, &scratch)) ||
         (rc = dalloc(&d_packbits, (size_t)std::max<int64_t>(n_words, 1), &scratch))) {
         free_scratch();
         return rc;
@@ -907,7 +924,7 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
         fill_i32_kernel<<<g, 256, 0, st>>>(d_seg_hi, ns, INT_MIN);
         ck(cudaGetLastError());
     }
-    ck(cudaMemsetAsync(d_flag, 0, 4, st));
+    ck(cudaMemsetAsync(d_flag, 0, 8, st));
     ck(cudaMemsetAsync(d_pub_counts, 0, MC_PUB_COUNTS * 8, st));
     // Planes: the upload pass writes sessions [0, n); only the padding up to
     // the stride needs clearing.
@@ -935,9 +952,14 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
         pack_counts_kernel<<<grid, 256, 0, st>>>(m->d_cnt, m->d_cnt16, qd_alloc);
         ck(cudaGetLastError());
     }
-    int flag = 0;
+    if (n_seg > 1) {
+        const int g = (int)std::min<int64_t>((n_seg + 255) / 256, (int64_t)4 * m->n_sm);
+        seg_order_kernel<<<g, 256, 0, st>>>(n_seg, d_seg_lo, d_seg_hi, d_flag + 1);
+        ck(cudaGetLastError());
+    }
+    int flags[2] = {0, 0};  // [0] an index outside [0, n_qd), [1] segments out of order
     std::vector<unsigned long long> pub_counts(MC_PUB_COUNTS, 0);
-    ck(cudaMemcpyAsync(&flag, d_flag, 4, cudaMemcpyDeviceToHost, st));
+    ck(cudaMemcpyAsync(flags, d_flag, 8, cudaMemcpyDeviceToHost, st));
     ck(cudaMemcpyAsync(pub_counts.data(), d_pub_counts, pub_counts.size() * 8, cudaMemcpyDeviceToHost, st));
     m->packbits.assign((size_t)n_words, 0u);
     if (n_words) ck(cudaMemcpyAsync(m->packbits.data(), d_packbits, (size_t)n_words * 4, cudaMemcpyDeviceToHost, st));
@@ -950,7 +972,7 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     ck(cudaStreamSynchronize(st));
     free_scratch();
     if (e != cudaSuccess) return cuda_fail("model_upload", e);
-    if (flag) {
+    if (flags[0]) {
         m->free_train();
         return set_error(MC_ERR_INVALID, "model_upload: a parameter index is outside [0, n_qd)");
     }
@@ -970,14 +992,10 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     }
 
     // Fused path precondition: per-query qd ranges disjoint and increasing.
-    m->fused_ok = true;
-    for (int64_t g = 1; g < n_seg; g++)
-        if (m->seg_lo[(size_t)g] < m->seg_hi[(size_t)g - 1]) {
-            m->fused_ok = false;
-            m->fused_reason = "sessions are not grouped by query with per-query contiguous parameter indices "
-                              "(as Dataset::parse_dataset leaves them)";
-            break;
-        }
+    m->fused_ok = !flags[1];
+    if (!m->fused_ok)
+        m->fused_reason = "sessions are not grouped by query with per-query contiguous parameter indices "
+                          "(as Dataset::parse_dataset leaves them)";
 
     // Public constants: prior plus the parts fixed by the click pattern.
     std::vector<double> pconst((size_t)(2 * m->n_pub), 0.0);
