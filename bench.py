@@ -487,6 +487,9 @@ def run_batched(args, rank: int, world: int, local: int):
     stream = torch.cuda.Stream()
     batch = api.Batch(models)
     n_fits, n_tiles, _ = batch.info()
+    n_count_fits = sum(1 for cm in models if cm.fused_path()[0] == "counts")
+    # per iteration: the tile launch (DBN/CCM fits) and the batched count launch (PBM/UBM fits)
+    launches_per_iteration = int(n_tiles > 0) + int(n_count_fits > 0)
 
     def timed(fn, steps):
         torch.cuda.synchronize()
@@ -517,12 +520,13 @@ def run_batched(args, rank: int, world: int, local: int):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_batch,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: per fit 1k queries Zipf(1.1), 20-doc pools, PBM clicks; sizes log-uniform 1k..500k",
-            "config": {"workload": f"{n_fits} fits, {int(sizes.sum())} sessions ({n_train} training), one launch per "
-                                   "iteration for all fits", "tiles": n_tiles, "prep_s": round(prep_s, 2)},
+            "config": {"workload": f"{n_fits} fits, {int(sizes.sum())} sessions ({n_train} training), per iteration "
+                                   "one tile launch for the DBN fits and one count launch for the PBM/UBM fits",
+                       "tiles": n_tiles, "count_path_fits": n_count_fits, "prep_s": round(prep_s, 2)},
             "separate_fused": {"value": n_train / (ms_sep / 1000.0), "ms_per_step": ms_sep},
             "separate_plain": {"value": n_train / (ms_plain / 1000.0), "ms_per_step": ms_plain,
                                "batched_speedup": ms_plain / ms_batch},
-            "gpu_launches": args.steps, "clocks": clk,
+            "gpu_launches": args.steps * launches_per_iteration, "clocks": clk,
         }
         print(json.dumps(line), flush=True)
 

@@ -234,9 +234,11 @@ void mc_model_destroy(mc_model* m);
  * ------------------------------------------------------------------------- */
 typedef struct mc_batch mc_batch;
 
-/* The models must be uploaded and on one device; every model is given the
- * first model's tile shape.  Models keep their own parameters and may still be
- * used alone; they must not be re-uploaded or reconfigured while the batch
+/* The models must be uploaded and on one device.  Models on the tile path
+ * (mc_model_fused_path = 0) share one persistent tile launch and are given the
+ * first such model's tile shape; models on the count path (PBM, UBM) share
+ * one batched count launch.  Models keep their own parameters and may still
+ * be used alone; they must not be re-uploaded or reconfigured while the batch
  * exists. */
 int mc_batch_create(int n_models, mc_model* const* models, mc_batch** out);
 
@@ -244,6 +246,8 @@ int mc_batch_create(int n_models, mc_model* const* models, mc_batch** out);
  * replayed.  NULL stream = internal stream, synchronous. */
 int mc_batch_em(mc_batch* b, int32_t n_iterations, void* stream);
 
+/* n_tiles: tiles of the tile launch; mixed_models: its tile fits are of more
+ * than one model type (the model-generic kernel runs). */
 int mc_batch_info(const mc_batch* b, int32_t* n_models, int32_t* n_tiles, int32_t* mixed_models);
 
 void mc_batch_destroy(mc_batch* b);

@@ -196,12 +196,16 @@ cudaError_t build_counts(int model, int64_t n, int64_t stride, int64_t n_qd, con
 // coalesced entry reads, a next-qd prefetch and register bins for PBM were
 // all slower at 22.6M qd: the kernel is bound by the shared-memory pipe and
 // lane divergence, not by DRAM latency.)
-__global__ void __launch_bounds__(256, 8) em_counts_kernel(const FitDev* __restrict__ fp, const uint32_t* __restrict__ off,
-                                                           const uint32_t* __restrict__ ent) {
+//
+// The block takes qd q_first, q_first + q_step, ... below q_end; the fit's
+// iteration is done by n_blocks blocks, and the last of them to finish runs
+// the public M-step.
+__device__ __forceinline__ void count_iteration(const FitDev& f, const uint32_t* __restrict__ off,
+                                                const uint32_t* __restrict__ ent, int64_t q_first, int64_t q_end,
+                                                int64_t q_step, unsigned n_blocks) {
     __shared__ float e[64];
     __shared__ float wbin[8][64];
     __shared__ int s_last, s_it;
-    const FitDev& f = *fp;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int n_pub = f.n_pub;
     if (tid == 0) s_it = *(volatile int*)f.iter;
@@ -210,9 +214,7 @@ __global__ void __launch_bounds__(256, 8) em_counts_kernel(const FitDev* __restr
     if (tid < 64) e[tid] = tid < n_pub ? f.pub_theta[(s_it & 1) * MC_MAX_PUB + tid] : 0.0f;
     __syncthreads();
     float* mybin = wbin[warp];
-    const int64_t n_qd = f.n_qd;
-    const int64_t step = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + tid; q < n_qd; q += step) {
+    for (int64_t q = q_first; q < q_end; q += q_step) {
         const float a = f.atr[q];
         const uint2 c = f.cnt[q];
         const uint32_t i1 = __ldg(off + q + 1);
@@ -238,7 +240,7 @@ __global__ void __launch_bounds__(256, 8) em_counts_kernel(const FitDev* __restr
     }
     __threadfence();
     __syncthreads();
-    if (tid == 0) s_last = atomicAdd(f.tiles_done, 1u) + 1 == gridDim.x;
+    if (tid == 0) s_last = atomicAdd(f.tiles_done, 1u) + 1 == n_blocks;
     __syncthreads();
     if (!s_last) return;
     // Last block: public M-step.
@@ -260,12 +262,46 @@ __global__ void __launch_bounds__(256, 8) em_counts_kernel(const FitDev* __restr
     }
 }
 
+// One fit: blocks stride over its qd.
+__global__ void __launch_bounds__(256, 8) em_counts_kernel(const FitDev* __restrict__ fp, const uint32_t* __restrict__ off,
+                                                           const uint32_t* __restrict__ ent) {
+    const FitDev& f = *fp;
+    count_iteration(f, off, ent, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, f.n_qd,
+                    (int64_t)gridDim.x * blockDim.x, gridDim.x);
+}
+
 cudaError_t launch_em_counts(const FitDev* fit, const uint32_t* off, const uint32_t* ent, int64_t n_qd, int n_sm,
                              cudaStream_t st) {
     const int64_t blocks = (n_qd + 255) / 256;
     int g = (int)(blocks < 8 * n_sm ? blocks : 8 * n_sm);
     if (g < 1) g = 1;
     em_counts_kernel<<<g, 256, 0, st>>>(fit, off, ent);
+    return cudaGetLastError();
+}
+
+// Many fits in one launch: fit i owns blocks [blk_begin, blk_begin + n_blocks),
+// each a contiguous chunk of kCountChunk of its qd, so a block serves one fit
+// and the fit's last block runs its public M-step.
+__global__ void __launch_bounds__(256, 6) em_counts_batch_kernel(const CountFitDev* __restrict__ fits, int n_fits) {
+    __shared__ int s_fit;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = n_fits - 1;  // last fit with blk_begin <= blockIdx.x
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (fits[mid].blk_begin <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
+        }
+        s_fit = lo;
+    }
+    __syncthreads();
+    const CountFitDev cf = fits[s_fit];
+    const int64_t q0 = (int64_t)((int)blockIdx.x - cf.blk_begin) * kCountChunk;
+    const int64_t q1 = q0 + kCountChunk < cf.n_qd ? q0 + kCountChunk : cf.n_qd;
+    count_iteration(*cf.fit, cf.off, cf.ent, q0 + threadIdx.x, q1, blockDim.x, (unsigned)cf.n_blocks);
+}
+
+cudaError_t launch_em_counts_batch(const CountFitDev* fits, int n_fits, int total_blocks, cudaStream_t st) {
+    if (n_fits == 0 || total_blocks == 0) return cudaSuccess;
+    em_counts_batch_kernel<<<total_blocks, 256, 0, st>>>(fits, n_fits);
     return cudaGetLastError();
 }
 

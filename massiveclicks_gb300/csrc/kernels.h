@@ -24,6 +24,17 @@ cudaError_t build_counts(int model, int64_t n, int64_t stride, int64_t n_qd, con
                          int n_sm, cudaStream_t st, uint32_t** off, uint32_t** ent, int64_t* n_entries, int* usable);
 cudaError_t launch_em_counts(const FitDev* fit, const uint32_t* off, const uint32_t* ent, int64_t n_qd, int n_sm,
                              cudaStream_t st);
+// Batched count path: fit i takes blocks [blk_begin, blk_begin + n_blocks),
+// one chunk of kCountChunk qd each (n_blocks = ceil(n_qd / kCountChunk)).
+constexpr int kCountChunk = 2048;
+struct CountFitDev {
+    const FitDev* fit;
+    const uint32_t* off;
+    const uint32_t* ent;
+    int64_t n_qd;
+    int blk_begin, n_blocks;
+};
+cudaError_t launch_em_counts_batch(const CountFitDev* fits, int n_fits, int total_blocks, cudaStream_t st);
 cudaError_t launch_pack_tiles(int model, TileDev* tiles, int n_tiles, int window_max, int max_tile_sessions, const int32_t* planes,
                               int64_t stride, const uint16_t* click, unsigned char* tblk, int* status, int n_sm,
                               cudaStream_t st);

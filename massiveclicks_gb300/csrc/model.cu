@@ -1449,23 +1449,31 @@ struct mc_batch {
     TileDev* d_tiles = nullptr;
     SplitDev* d_splits = nullptr;
     WorkState* d_ws = nullptr;
+    // Fits on the count path (PBM/UBM) run in one batched count launch.
+    CountFitDev* d_cfits = nullptr;
+    int n_cfits = 0, count_blocks = 0;
     mc_model::GraphSlot graphs[2];
     cudaStream_t own_stream = nullptr;
     int64_t bytes = 0;
 
     void release() {
         for (auto& g : graphs) { if (g.exec) cudaGraphExecDestroy(g.exec); g.exec = nullptr; g.iters = -1; }
-        settle(d_fits, d_tiles, d_splits, d_ws);
-        dfree(d_fits); dfree(d_tiles); dfree(d_splits); dfree(d_ws);
+        settle(d_fits, d_tiles, d_splits, d_ws, d_cfits);
+        dfree(d_fits); dfree(d_tiles); dfree(d_splits); dfree(d_ws); dfree(d_cfits);
         if (own_stream) cudaStreamDestroy(own_stream);
         own_stream = nullptr;
     }
 };
 
+// One iteration of every fit: the tile kernel over the tile fits, then the
+// batched count kernel over the count-path fits.
 static int batch_launch_loop(mc_batch* b, int iters, cudaStream_t st) {
-    for (int i = 0; i < iters; i++)
-        CK(launch_em_fused(b->kernel_model, b->d_fits, b->d_tiles, b->n_tiles, b->d_splits, b->d_ws, b->wqd, b->spt,
-                           b->stages, b->grid, b->block, st));
+    for (int i = 0; i < iters; i++) {
+        if (b->n_tiles)
+            CK(launch_em_fused(b->kernel_model, b->d_fits, b->d_tiles, b->n_tiles, b->d_splits, b->d_ws, b->wqd, b->spt,
+                               b->stages, b->grid, b->block, st));
+        if (b->n_cfits) CK(launch_em_counts_batch(b->d_cfits, b->n_cfits, b->count_blocks, st));
+    }
     return MC_OK;
 }
 
@@ -1478,11 +1486,16 @@ extern "C" int mc_batch_create(int n_models, mc_model* const* models, mc_batch**
         if (!m->fused_ok) return set_error(MC_ERR_INVALID, "batch_create: model " + std::to_string(i) + ": " + m->fused_reason);
         if (m->device != models[0]->device) return set_error(MC_ERR_INVALID, "batch_create: models on different devices");
     }
+    CK(cudaSetDevice(models[0]->device));
+    // Count-path fits (PBM/UBM with their counts) need no tiles; the others
+    // share one tile shape: the first tile fit's.
+    auto on_counts = [](const mc_model* m) { return m->d_coff != nullptr; };
     mc_model* m0 = models[0];
-    CK(cudaSetDevice(m0->device));
-    // One tile shape for the whole launch: the first model's.
-    for (int i = 1; i < n_models; i++) {
+    for (int i = 0; i < n_models; i++)
+        if (!on_counts(models[i])) { m0 = models[i]; break; }
+    for (int i = 0; i < n_models; i++) {
         mc_model* m = models[i];
+        if (on_counts(m) || m == m0) continue;
         if (m->spt != m0->spt || m->wqd != m0->wqd || m->block != m0->block) {
             int rc = mc_model_configure(m, m0->spt, m0->wqd, m0->block);
             if (rc) return rc;
@@ -1500,11 +1513,27 @@ extern "C" int mc_batch_create(int n_models, mc_model* const* models, mc_batch**
     std::vector<FitDev> fits;
     std::vector<TileDev> tiles;
     std::vector<SplitDev> splits;
+    std::vector<CountFitDev> cfits;
     for (int i = 0; i < n_models; i++) {
         mc_model* m = models[i];
+        // fits[] keeps one entry per model, so a tile's fit index is the model's.
+        fits.push_back(m->make_desc());
+        if (on_counts(m)) {
+            CountFitDev c{};
+            c.fit = m->d_fit;
+            c.off = m->d_coff;
+            c.ent = m->d_cent;
+            c.n_qd = m->n_qd;
+            c.blk_begin = b->count_blocks;
+            c.n_blocks = (int)((m->n_qd + kCountChunk - 1) / kCountChunk);
+            if (c.n_blocks == 0) continue;
+            b->count_blocks += c.n_blocks;
+            cfits.push_back(c);
+            continue;
+        }
         if (m->model != b->kernel_model) b->kernel_model = -1;
         if (int rc = m->ensure_tiles()) { delete b; return rc; }
-        fits.push_back(m->make_desc());
+        fits.back() = m->make_desc();
         std::vector<TileDev> t((size_t)m->n_tiles);
         std::vector<SplitDev> sp((size_t)m->n_splits);
         cudaError_t e = cudaSuccess;
@@ -1520,18 +1549,26 @@ extern "C" int mc_batch_create(int n_models, mc_model* const* models, mc_batch**
         splits.insert(splits.end(), sp.begin(), sp.end());
     }
     b->n_tiles = (int)tiles.size();
+    b->n_cfits = (int)cfits.size();
     int rc;
     if ((rc = dalloc(&b->d_fits, fits.size(), &b->bytes)) || (rc = dalloc(&b->d_tiles, tiles.size(), &b->bytes)) ||
-        (rc = dalloc(&b->d_splits, splits.size(), &b->bytes)) || (rc = dalloc(&b->d_ws, 1, &b->bytes))) {
+        (rc = dalloc(&b->d_splits, splits.size(), &b->bytes)) || (rc = dalloc(&b->d_ws, 1, &b->bytes)) ||
+        (rc = dalloc(&b->d_cfits, cfits.size(), &b->bytes))) {
         b->release();
         delete b;
         return rc;
     }
     cudaError_t e = cudaMemcpy(b->d_fits, fits.data(), fits.size() * sizeof(FitDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !cfits.empty())
+        e = cudaMemcpy(b->d_cfits, cfits.data(), cfits.size() * sizeof(CountFitDev), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !tiles.empty()) e = cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !splits.empty()) e = cudaMemcpy(b->d_splits, splits.data(), splits.size() * sizeof(SplitDev), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(b->d_ws, 0, sizeof(WorkState));
     if (e != cudaSuccess) { b->release(); delete b; return cuda_fail("batch_create", e); }
+    if (b->n_tiles == 0) {  // count-path fits only
+        *out = b;
+        return MC_OK;
+    }
     // Shared memory and occupancy of the common launch.
     int optin = 0;
     e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
@@ -1567,7 +1604,7 @@ extern "C" int mc_batch_em(mc_batch* b, int32_t iters, void* stream) {
         if (!b->own_stream) CK(cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking));
         st = b->own_stream;
     }
-    if (iters == 0 || b->n_tiles == 0) return MC_OK;
+    if (iters == 0 || (b->n_tiles == 0 && b->n_cfits == 0)) return MC_OK;
     const int full = iters / kGraphChunk, rem = iters % kGraphChunk;
     for (int pass = 0; pass < 2; pass++) {
         int len = pass == 0 ? kGraphChunk : rem;

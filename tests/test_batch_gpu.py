@@ -77,3 +77,52 @@ def test_batch_rejects_models_without_sessions():
     cm = api.ClickModel.create(0)
     with pytest.raises(api._capi.MCError):
         api.Batch([cm])
+
+
+def _fit_all(parts):
+    models = []
+    for model, train, n_qd in parts:
+        cm = api.ClickModel.create(model)
+        cm.upload(train, n_qd)
+        models.append(cm)
+    return models
+
+
+def test_count_path_fits_batch_without_tiles():
+    """PBM and UBM fits take the batched count launch and build no tiles."""
+    parts = []
+    for name, model in [("pbm_pbmclicks", 0), ("ubm_dbnclicks", 3), ("dbn_ccmclicks", 0)]:
+        c = load_case(name)
+        parts.append((model, _sset(c, "train"), int(c["n_qd"])))
+    cfg = api.synth_config(1, n_sessions=40000, n_queries=1000, seed=4242)
+    q, d, m = api.synth_sessions(cfg)
+    ds = api.Dataset.from_sessions(q, d, m, 0.0)
+    parts.append((3, ds.train, ds.n_qd))
+    models = _fit_all(parts)
+    b = api.Batch(models)
+    n_models, n_tiles, mixed = b.info()
+    assert (n_models, n_tiles, mixed) == (len(parts), 0, 0)
+    b.em(6)
+    for (model, train, n_qd), cm in zip(parts, models):
+        f = bindings.OracleFit("f64", model, 0, train.query, train.pidx, train.click, n_qd)
+        f.run(6)
+        _close(cm.get_parameters(), f.values(), PARAM_RTOL, PARAM_ATOL, f"count batch m{model}")
+    b.close()
+
+
+def test_batch_of_both_paths_runs_the_specialised_tile_kernel():
+    """DBN tile fits next to PBM/UBM count fits: the tile launch holds DBN only."""
+    parts = []
+    for name, model in [("dbn_dbnclicks", 2), ("pbm_pbmclicks", 0), ("ubm_dbnclicks", 3), ("edge", 2)]:
+        c = load_case(name)
+        parts.append((model, _sset(c, "train"), int(c["n_qd"])))
+    models = _fit_all(parts)
+    b = api.Batch(models)
+    n_models, n_tiles, mixed = b.info()
+    assert n_models == len(parts) and n_tiles > 0 and not mixed
+    b.em(5)
+    for (model, train, n_qd), cm in zip(parts, models):
+        f = bindings.OracleFit("f64", model, 0, train.query, train.pidx, train.click, n_qd)
+        f.run(5)
+        _close(cm.get_parameters(), f.values(), PARAM_RTOL, PARAM_ATOL, f"two-path batch m{model}")
+    b.close()
