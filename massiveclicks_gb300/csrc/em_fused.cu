@@ -446,12 +446,15 @@ __device__ __forceinline__ void estep_ccm(const Src& src, const Sink& sink, int 
             E = cont;
             P = 1.0f;
         } else {
-            float D = __fdividef(1.0f, P - t1 * E * (1.0f - R));
-            t[0] += t1 * R * E * D;
-            t[1] += E * (1.0f - t1 * (1.0f - R)) * D;
+            // Unclicked rank after the last click (te = t1 E, u = te (1 - R)).
+            const float te = t1 * E;
+            const float u = te * (1.0f - R);
+            const float D = __fdividef(1.0f, P - u);
+            t[0] += te * R * D;
+            t[1] += (E - u) * D;
             sink.add(rls[r], 0, __fdividef((1.0f - eps) * a[r], 1.0f - eps * car[r]));
             P = P - a[r] * E;
-            E = E * t1 * ia;
+            E = te * ia;
             rescale(P, E);
         }
         eps *= ia * t1 + a[r] * (ia * t2 + a[r] * t3);
