@@ -322,7 +322,12 @@ def run_ours(args, rank: int, world: int, local: int):
     # (22 B: uint16 window indices x10 + clicks) and per qd 24 B (atr, sat,
     # counts read; atr, sat written).
     path, n_entries = cm.fused_path()
-    if path == "counts":
+    if path == "dense":
+        # PBM dense kernel: 20 B of uint16 counts by rank per qd; 8 B occurrence/click
+        # counts, 4 B value read and 4 B value written.
+        design_bytes = 36 * n_qd
+        design_model = "dense count path: 36 B/qd (uint16 counts x10, occurrences/clicks, value read and write)"
+    elif path == "counts":
         # PBM/UBM count kernel: 4 B per count entry; per qd 4 B offset, 8 B
         # occurrence/click counts, 4 B value read and 4 B value written.
         design_bytes = 4 * n_entries + 20 * n_qd
@@ -487,7 +492,7 @@ def run_batched(args, rank: int, world: int, local: int):
     stream = torch.cuda.Stream()
     batch = api.Batch(models)
     n_fits, n_tiles, _ = batch.info()
-    n_count_fits = sum(1 for cm in models if cm.fused_path()[0] == "counts")
+    n_count_fits = sum(1 for cm in models if cm.fused_path()[0] in ("counts", "dense"))
     # per iteration: the tile launch (DBN/CCM fits) and the batched count launch (PBM/UBM fits)
     launches_per_iteration = int(n_tiles > 0) + int(n_count_fits > 0)
 

@@ -208,8 +208,9 @@ int mc_model_em_trace(mc_model* m, int32_t n_iterations, double* train_ll, void*
 
 /* Which kernel one fused iteration of the uploaded model launches: *path = 0
  * the tile kernel over the sessions, 1 the count kernel over the per-(qd, key)
- * occurrence counts built at upload (PBM and UBM); *n_entries = the number of
- * count entries (0 on the tile path).  The reference has one E-step kernel per
+ * occurrence counts built at upload (UBM, and PBM when a count exceeds 16
+ * bits), 2 the PBM kernel over dense uint16 [n_qd][10] counts by rank;
+ * *n_entries = the number of (qd, key) count entries (0 on the tile path).  The reference has one E-step kernel per
  * model (pbm.cu:191-253, ubm.cu:185-247); this reports which equivalent runs. */
 int mc_model_fused_path(const mc_model* m, int32_t* path, int64_t* n_entries);
 

@@ -269,10 +269,11 @@ class ClickModel:
     def fused_path(self) -> tuple:
         """("tiles", 0) when a fused iteration runs the tile kernel over the
         sessions, ("counts", n_entries) when it runs the count kernel over the
-        per-(qd, key) occurrence counts (PBM and UBM)."""
+        per-(qd, key) occurrence counts (UBM), ("dense", n_entries) for the PBM
+        kernel over dense per-rank counts."""
         p, n = C.c_int32(), C.c_int64()
         check(_capi.load().mc_model_fused_path(self._h, C.byref(p), C.byref(n)))
-        return ("counts" if p.value == 1 else "tiles", int(n.value))
+        return ({0: "tiles", 1: "counts", 2: "dense"}[p.value], int(n.value))
 
     def memory(self) -> int:
         b = C.c_int64()

@@ -90,6 +90,21 @@ __global__ void count_offsets_kernel(int64_t n_qd, int64_t runs, const K* __rest
     }
 }
 
+// PBM: dense[qd * 10 + rank] = count of run i (every PBM key is alive and
+// unique per (qd, rank)); flags a count above 65535.
+template <class K>
+__global__ void count_dense_kernel(int64_t runs, const K* __restrict__ uniq, const uint32_t* __restrict__ counts,
+                                   uint16_t* __restrict__ dense, int* overflow) {
+    const int64_t step = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < runs; i += step) {
+        const uint32_t c = counts[i];
+        if (c > 0xFFFFu) { atomicOr(overflow, 1); continue; }
+        const int64_t q = (int64_t)(uniq[i] >> 7);
+        const int r = (int)((uniq[i] >> 1) & K(63));
+        dense[q * MC_R + r] = (uint16_t)c;
+    }
+}
+
 static int grid_for(int64_t n, int n_sm) {
     int64_t b = (n + 255) / 256;
     int g = (int)(b < 16 * n_sm ? b : 16 * n_sm);
@@ -107,13 +122,14 @@ static cudaError_t tmp_alloc(T** p, size_t count) {
 template <class K>
 static cudaError_t build_counts_t(int model, int64_t n, int64_t stride, int64_t n_qd, const int32_t* planes,
                                   const uint16_t* click, int n_sm, cudaStream_t st, uint32_t** off_out,
-                                  uint32_t** ent_out, int64_t* n_entries, int* usable) {
+                                  uint32_t** ent_out, int64_t* n_entries, uint16_t** dense_out, int* usable) {
     const int64_t nk = n * MC_R;
     K *keys = nullptr, *alt = nullptr;
     uint32_t* counts = nullptr;
-    int64_t* d_small = nullptr;  // [0] run count, [1] overflow flag
+    int64_t* d_small = nullptr;  // [0] run count, [1] overflow flags: CSR (low word), dense (high word)
     void* temp = nullptr;
     uint32_t *off = nullptr, *ent = nullptr;
+    uint16_t* dense = nullptr;
     cudaError_t e = cudaSuccess;
     auto ck = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
     auto release = [&]() {  // after the stream has drained
@@ -153,42 +169,56 @@ static cudaError_t build_counts_t(int model, int64_t n, int64_t stride, int64_t 
     }
     ck(tmp_alloc(&off, (size_t)n_qd + 1));
     ck(tmp_alloc(&ent, (size_t)(runs > 0 ? runs : 1)));
+    if (model == PBM && dense_out) ck(tmp_alloc(&dense, (size_t)n_qd * MC_R));
+    int* overflow = reinterpret_cast<int*>(d_small + 1);
     if (e == cudaSuccess) {
         ck(cudaMemsetAsync(off, 0, ((size_t)n_qd + 1) * sizeof(uint32_t), st));
-        int* overflow = reinterpret_cast<int*>(d_small + 1);
         count_entries_kernel<K><<<grid_for(runs, n_sm), 256, 0, st>>>(runs, uniq, counts, ent, overflow);
         ck(cudaGetLastError());
         count_offsets_kernel<K><<<grid_for(runs, n_sm), 256, 0, st>>>(n_qd, runs, uniq, off);
         ck(cudaGetLastError());
+        if (dense) {
+            ck(cudaMemsetAsync(dense, 0, (size_t)n_qd * MC_R * sizeof(uint16_t), st));
+            count_dense_kernel<K><<<grid_for(runs, n_sm), 256, 0, st>>>(runs, uniq, counts, dense, overflow + 1);
+            ck(cudaGetLastError());
+        }
     }
-    int overflow = 0;
-    ck(cudaMemcpyAsync(&overflow, d_small + 1, 4, cudaMemcpyDeviceToHost, st));
+    int flags[2] = {0, 0};
+    ck(cudaMemcpyAsync(flags, overflow, 8, cudaMemcpyDeviceToHost, st));
     ck(cudaStreamSynchronize(st));
     release();
-    if (e != cudaSuccess || overflow) {
+    if (e != cudaSuccess || flags[0]) {
         mch::dev_free(off);
         mch::dev_free(ent);
+        mch::dev_free(dense);
         return e;  // on overflow: success without the count path
+    }
+    if (flags[1]) {  // a count above 16 bits: the entries only
+        mch::dev_free(dense);
+        dense = nullptr;
     }
     *off_out = off;
     *ent_out = ent;
     *n_entries = runs;
+    if (dense_out) *dense_out = dense;
     *usable = 1;
     return cudaSuccess;
 }
 
 cudaError_t build_counts(int model, int64_t n, int64_t stride, int64_t n_qd, const int32_t* planes, const uint16_t* click,
                          int n_sm, cudaStream_t st, uint32_t** off_out, uint32_t** ent_out, int64_t* n_entries,
-                         int* usable) {
+                         uint16_t** dense_out, int* usable) {
     *off_out = nullptr;
     *ent_out = nullptr;
     *n_entries = 0;
+    if (dense_out) *dense_out = nullptr;
     *usable = 0;
     if (n * MC_R >= ((int64_t)1 << 32) || n_qd >= ((int64_t)1 << 56)) return cudaSuccess;  // keep the tile path
     if (n_qd <= ((int64_t)1 << 25) - 2)
-        return build_counts_t<uint32_t>(model, n, stride, n_qd, planes, click, n_sm, st, off_out, ent_out, n_entries, usable);
+        return build_counts_t<uint32_t>(model, n, stride, n_qd, planes, click, n_sm, st, off_out, ent_out, n_entries,
+                                        dense_out, usable);
     return build_counts_t<unsigned long long>(model, n, stride, n_qd, planes, click, n_sm, st, off_out, ent_out, n_entries,
-                                              usable);
+                                              dense_out, usable);
 }
 
 // One thread per qd: its entries, its M-step in place; the public terms of the
@@ -197,6 +227,36 @@ cudaError_t build_counts(int model, int64_t n, int64_t stride, int64_t n_qd, con
 // all slower at 22.6M qd: the kernel is bound by the shared-memory pipe and
 // lane divergence, not by DRAM latency.)
 //
+// After a block has added its public partial sums: the last of the fit's
+// n_blocks blocks to finish runs the public M-step into the other half of the
+// double buffer, clears the bins and the block counter and advances iter.
+__device__ __forceinline__ void public_finish(const FitDev& f, int s_it, unsigned n_blocks) {
+    __shared__ int s_last;
+    const int tid = threadIdx.x;
+    const int n_pub = f.n_pub;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(f.tiles_done, 1u) + 1 == n_blocks;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const int nb = (s_it + 1) & 1;
+    if (tid < n_pub) {
+        const double num = f.pub_const[2 * tid] + __ldcg(f.pub_bins + 2 * tid);
+        const double den = f.pub_const[2 * tid + 1] + __ldcg(f.pub_bins + 2 * tid + 1);
+        const double v = num / den;
+        f.pub_theta[nb * MC_MAX_PUB + tid] = (float)(v < (double)MC_TOP ? v : (double)MC_TOP);
+        f.pub_bins[2 * tid] = 0.0;
+        f.pub_bins[2 * tid + 1] = 0.0;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        *f.tiles_done = 0;
+        __threadfence();
+        *(volatile int*)f.iter = s_it + 1;
+    }
+}
+
 // The block takes qd q_first, q_first + q_step, ... below q_end; the fit's
 // iteration is done by n_blocks blocks, and the last of them to finish runs
 // the public M-step.
@@ -205,7 +265,7 @@ __device__ __forceinline__ void count_iteration(const FitDev& f, const uint32_t*
                                                 int64_t q_step, unsigned n_blocks) {
     __shared__ float e[64];
     __shared__ float wbin[8][64];
-    __shared__ int s_last, s_it;
+    __shared__ int s_it;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int n_pub = f.n_pub;
     if (tid == 0) s_it = *(volatile int*)f.iter;
@@ -238,28 +298,7 @@ __device__ __forceinline__ void count_iteration(const FitDev& f, const uint32_t*
         for (int w = 0; w < 8; w++) s += (double)wbin[w][tid];
         if (s != 0.0) atomicAdd(f.pub_bins + 2 * tid, s);
     }
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) s_last = atomicAdd(f.tiles_done, 1u) + 1 == n_blocks;
-    __syncthreads();
-    if (!s_last) return;
-    // Last block: public M-step.
-    __threadfence();
-    const int nb = (s_it + 1) & 1;
-    if (tid < n_pub) {
-        const double num = f.pub_const[2 * tid] + __ldcg(f.pub_bins + 2 * tid);
-        const double den = f.pub_const[2 * tid + 1] + __ldcg(f.pub_bins + 2 * tid + 1);
-        const double v = num / den;
-        f.pub_theta[nb * MC_MAX_PUB + tid] = (float)(v < (double)MC_TOP ? v : (double)MC_TOP);
-        f.pub_bins[2 * tid] = 0.0;
-        f.pub_bins[2 * tid + 1] = 0.0;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        *f.tiles_done = 0;
-        __threadfence();
-        *(volatile int*)f.iter = s_it + 1;
-    }
+    public_finish(f, s_it, n_blocks);
 }
 
 // One fit: blocks stride over its qd.
@@ -276,6 +315,71 @@ cudaError_t launch_em_counts(const FitDev* fit, const uint32_t* off, const uint3
     int g = (int)(blocks < 8 * n_sm ? blocks : 8 * n_sm);
     if (g < 1) g = 1;
     em_counts_kernel<<<g, 256, 0, st>>>(fit, off, ent);
+    return cudaGetLastError();
+}
+
+// PBM from dense counts: row q holds the unclicked occurrences of qd q at
+// ranks 0..9 (uint16), so every thread runs the same ten-rank loop and the
+// rank sums stay in registers (no shared atomics); warp sums, then FP64 block
+// sums, then one global atomic per rank per block.
+__global__ void __launch_bounds__(256, 6) em_counts_pbm_dense_kernel(const FitDev* __restrict__ fp,
+                                                                    const uint16_t* __restrict__ dense) {
+    __shared__ float wsum[8][MC_R];
+    __shared__ float e[MC_R];  // read with one address per warp (broadcast)
+    __shared__ int s_it;
+    const FitDev& f = *fp;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_it = *(volatile int*)f.iter;
+    __syncthreads();
+    if (tid < MC_R) e[tid] = f.pub_theta[(s_it & 1) * MC_MAX_PUB + tid];
+    __syncthreads();
+    float acc[MC_R];
+#pragma unroll
+    for (int r = 0; r < MC_R; r++) acc[r] = 0.0f;
+    const int64_t n_qd = f.n_qd;
+    const int64_t step = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + tid; q < n_qd; q += step) {
+        const float a = f.atr[q];
+        const uint2 c = f.cnt[q];
+        const uint32_t* row = reinterpret_cast<const uint32_t*>(dense + q * MC_R);  // 20 B, 4-byte aligned
+        uint32_t w2[MC_R / 2];
+#pragma unroll
+        for (int j = 0; j < MC_R / 2; j++) w2[j] = __ldg(row + j);
+        float v0 = 0.0f;
+#pragma unroll
+        for (int r = 0; r < MC_R; r++) {
+            const uint32_t k = (r & 1) ? (w2[r >> 1] >> 16) : (w2[r >> 1] & 0xFFFFu);
+            if (k) {
+                const float ae = a * e[r];
+                const float w = (float)k * __fdividef(1.0f, 1.0f - ae);
+                v0 += w * (a - ae);
+                acc[r] += w * (e[r] - ae);
+            }
+        }
+        const float v = __fdividef(1.0f + (float)c.y + v0, 2.0f + (float)c.x);
+        f.atr[q] = v < MC_TOP ? v : MC_TOP;
+    }
+#pragma unroll
+    for (int r = 0; r < MC_R; r++) {
+        float v = acc[r];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) wsum[warp][r] = v;
+    }
+    __syncthreads();
+    if (tid < MC_R) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += (double)wsum[w][tid];
+        if (s != 0.0) atomicAdd(f.pub_bins + 2 * tid, s);
+    }
+    public_finish(f, s_it, gridDim.x);
+}
+
+cudaError_t launch_em_counts_pbm_dense(const FitDev* fit, const uint16_t* dense, int64_t n_qd, int n_sm, cudaStream_t st) {
+    const int64_t blocks = (n_qd + 255) / 256;
+    int g = (int)(blocks < 6 * n_sm ? blocks : 6 * n_sm);
+    if (g < 1) g = 1;
+    em_counts_pbm_dense_kernel<<<g, 256, 0, st>>>(fit, dense);
     return cudaGetLastError();
 }
 

@@ -20,8 +20,12 @@ cudaError_t launch_em_fused(int model, const FitDev* fits, const TileDev* tiles,
 // build_counts sorts the unclicked occurrences of the uploaded sessions into
 // per-qd entries (CSR: off[n_qd + 1], ent[n_entries]); *usable = 0 keeps the
 // tile path (sizes beyond the entry format).
+// For PBM, *dense (if dense is not null) also receives uint16 [n_qd][10]
+// counts by rank, or nullptr when a count exceeds 16 bits.
 cudaError_t build_counts(int model, int64_t n, int64_t stride, int64_t n_qd, const int32_t* planes, const uint16_t* click,
-                         int n_sm, cudaStream_t st, uint32_t** off, uint32_t** ent, int64_t* n_entries, int* usable);
+                         int n_sm, cudaStream_t st, uint32_t** off, uint32_t** ent, int64_t* n_entries,
+                         uint16_t** dense, int* usable);
+cudaError_t launch_em_counts_pbm_dense(const FitDev* fit, const uint16_t* dense, int64_t n_qd, int n_sm, cudaStream_t st);
 cudaError_t launch_em_counts(const FitDev* fit, const uint32_t* off, const uint32_t* ent, int64_t n_qd, int n_sm,
                              cudaStream_t st);
 // Batched count path: fit i takes blocks [blk_begin, blk_begin + n_blocks),

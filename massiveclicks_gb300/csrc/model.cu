@@ -341,6 +341,7 @@ struct mc_model {
     uint32_t* d_cnt16 = nullptr;
     uint32_t* d_coff = nullptr;  // PBM/UBM: per-qd entry offsets [n_qd + 1] of the count path
     uint32_t* d_cent = nullptr;  // PBM/UBM: entries (count << 7 | key << 1 | alive)
+    uint16_t* d_cdense = nullptr;  // PBM: uint16 [n_qd][10] counts by rank (when all fit 16 bits)
     int64_t n_cent = 0;
     float *d_atr = nullptr, *d_sat = nullptr, *d_pub_theta = nullptr;
     double *d_pub_bins = nullptr, *d_pub_const = nullptr, *d_split_bins = nullptr;
@@ -425,7 +426,7 @@ struct mc_model {
         free_tiles();
         free_plain();
         settle(d_pidx, d_click, d_atr, d_fit, d_grad);
-        dfree(d_pidx); dfree(d_click); dfree(d_cnt); dfree(d_cnt16); dfree(d_coff); dfree(d_cent); dfree(d_atr); dfree(d_sat); dfree(d_pub_theta);
+        dfree(d_pidx); dfree(d_click); dfree(d_cnt); dfree(d_cnt16); dfree(d_coff); dfree(d_cent); dfree(d_cdense); dfree(d_atr); dfree(d_sat); dfree(d_pub_theta);
         dfree(d_pub_bins); dfree(d_pub_const); dfree(d_tiles_done); dfree(d_iter); dfree(d_status);
         dfree(d_fit); dfree(d_ws); dfree(d_grad);
         bytes = test_bytes;
@@ -980,7 +981,7 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
         int usable = 0;
         int64_t n_ent = 0;
         e = build_counts(m->model, n, m->stride, n_qd, m->d_pidx, m->d_click, m->n_sm, st, &m->d_coff, &m->d_cent,
-                         &n_ent, &usable);
+                         &n_ent, &m->d_cdense, &usable);
         if (e != cudaSuccess) {
             m->free_train();
             return cuda_fail("model_upload", e);
@@ -988,6 +989,7 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
         if (usable) {
             m->n_cent = n_ent;
             m->bytes += (int64_t)sizeof(uint32_t) * ((n_qd + 1) + std::max<int64_t>(n_ent, 1));
+            if (m->d_cdense) m->bytes += (int64_t)sizeof(uint16_t) * n_qd * MC_R;
         }
     }
 
@@ -1096,6 +1098,7 @@ extern "C" int mc_model_get_config(const mc_model* m, int32_t* spt, int32_t* wqd
 // One fused iteration: PBM and UBM from their per-(qd, key) counts, the
 // other models (or sizes beyond the count format) through the tile kernel.
 static cudaError_t launch_fused_once(mc_model* m, cudaStream_t st) {
+    if (m->d_cdense) return launch_em_counts_pbm_dense(m->d_fit, m->d_cdense, m->n_qd, m->n_sm, st);
     if (m->d_coff) return launch_em_counts(m->d_fit, m->d_coff, m->d_cent, m->n_qd, m->n_sm, st);
     return launch_em_fused(m->model, m->d_fit, m->d_tiles, m->n_tiles, m->d_splits, m->d_ws, m->wqd, m->spt, m->stages,
                            m->grid, m->block, st);
@@ -1401,7 +1404,7 @@ extern "C" int mc_model_autotune(mc_model* m, void* stream) {
 extern "C" int mc_model_fused_path(const mc_model* m, int32_t* path, int64_t* n_entries) {
     if (!m || !path || !n_entries) return set_error(MC_ERR_INVALID, "model_fused_path: null argument");
     if (!m->uploaded) return set_error(MC_ERR_STATE, "model_fused_path: no training sessions uploaded");
-    *path = m->d_coff ? 1 : 0;
+    *path = m->d_cdense ? 2 : m->d_coff ? 1 : 0;
     *n_entries = m->d_coff ? m->n_cent : 0;
     return MC_OK;
 }
