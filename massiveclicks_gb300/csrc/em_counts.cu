@@ -263,17 +263,20 @@ __device__ __forceinline__ void public_finish(const FitDev& f, int s_it, unsigne
 __device__ __forceinline__ void count_iteration(const FitDev& f, const uint32_t* __restrict__ off,
                                                 const uint32_t* __restrict__ ent, int64_t q_first, int64_t q_end,
                                                 int64_t q_step, unsigned n_blocks) {
+    // Public bins: kBinCopies copies per warp, lane l adding to copy l % 8, so
+    // only lanes that share a copy and a key meet on one address.
+    constexpr int kBinCopies = 8;
     __shared__ float e[64];
-    __shared__ float wbin[8][64];
+    __shared__ float wbin[8][MC_UBM_SLOTS][kBinCopies];
     __shared__ int s_it;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int n_pub = f.n_pub;
     if (tid == 0) s_it = *(volatile int*)f.iter;
-    for (int k = tid; k < 8 * 64; k += blockDim.x) (&wbin[0][0])[k] = 0.0f;
+    for (int k = tid; k < 8 * MC_UBM_SLOTS * kBinCopies; k += blockDim.x) (&wbin[0][0][0])[k] = 0.0f;
     __syncthreads();
     if (tid < 64) e[tid] = tid < n_pub ? f.pub_theta[(s_it & 1) * MC_MAX_PUB + tid] : 0.0f;
     __syncthreads();
-    float* mybin = wbin[warp];
+    float* mybin = &wbin[warp][0][tid & (kBinCopies - 1)];
     for (int64_t q = q_first; q < q_end; q += q_step) {
         const float a = f.atr[q];
         const uint2 c = f.cnt[q];
@@ -286,7 +289,7 @@ __device__ __forceinline__ void count_iteration(const FitDev& f, const uint32_t*
             const float ae = a * ek;
             const float w = (float)(x >> 7) * __fdividef(1.0f, 1.0f - ae);
             v0 += w * (a - ae);
-            if (x & 1u) atomicAdd(mybin + k, w * (ek - ae));
+            if (x & 1u) atomicAdd(mybin + k * kBinCopies, w * (ek - ae));
         }
         // M-step, PBM and UBM in both modes: (1 + clicks + v0) / (2 + occurrences).
         const float v = __fdividef(1.0f + (float)c.y + v0, 2.0f + (float)c.x);
@@ -295,7 +298,8 @@ __device__ __forceinline__ void count_iteration(const FitDev& f, const uint32_t*
     __syncthreads();
     if (tid < n_pub) {
         double s = 0.0;
-        for (int w = 0; w < 8; w++) s += (double)wbin[w][tid];
+        for (int w = 0; w < 8; w++)
+            for (int c = 0; c < kBinCopies; c++) s += (double)wbin[w][tid][c];
         if (s != 0.0) atomicAdd(f.pub_bins + 2 * tid, s);
     }
     public_finish(f, s_it, n_blocks);
