@@ -85,3 +85,14 @@ def test_model_errors_without_device(native_lib):
     assert b"model type" in buf.value
     assert native_lib.mc_model_em(None, 1, 0, None) == 1
     assert native_lib.mc_model_param_count(None) == 0
+
+
+def test_device_cache_entry_points_without_device(native_lib):
+    """With nothing cached, the cache queries and release make no CUDA call."""
+    b = ctypes.c_int64(-1)
+    assert native_lib.mc_cache_bytes(-1, ctypes.byref(b)) == 0 and b.value == 0
+    assert native_lib.mc_empty_cache(-1, ctypes.byref(b)) == 0 and b.value == 0
+    assert native_lib.mc_empty_cache(0, None) == 0
+    assert native_lib.mc_cache_bytes(0, None) == 1  # null output rejected
+    h = ctypes.c_int32()
+    assert native_lib.mc_model_fused_path(None, ctypes.byref(h), ctypes.byref(b)) == 1
