@@ -259,13 +259,14 @@ __device__ __forceinline__ void public_finish(const FitDev& f, int s_it, unsigne
 
 // The block takes qd q_first, q_first + q_step, ... below q_end; the fit's
 // iteration is done by n_blocks blocks, and the last of them to finish runs
-// the public M-step.
+// the public M-step.  COPIES copies of each warp's public bins: lane l adds
+// to copy l % COPIES, so only lanes that share a copy and a key meet on one
+// shared-memory address.
+template <int COPIES>
 __device__ __forceinline__ void count_iteration(const FitDev& f, const uint32_t* __restrict__ off,
                                                 const uint32_t* __restrict__ ent, int64_t q_first, int64_t q_end,
                                                 int64_t q_step, unsigned n_blocks) {
-    // Public bins: kBinCopies copies per warp, lane l adding to copy l % 8, so
-    // only lanes that share a copy and a key meet on one address.
-    constexpr int kBinCopies = 8;
+    constexpr int kBinCopies = COPIES;
     __shared__ float e[64];
     __shared__ float wbin[8][MC_UBM_SLOTS][kBinCopies];
     __shared__ int s_it;
@@ -309,8 +310,8 @@ __device__ __forceinline__ void count_iteration(const FitDev& f, const uint32_t*
 __global__ void __launch_bounds__(256, 8) em_counts_kernel(const FitDev* __restrict__ fp, const uint32_t* __restrict__ off,
                                                            const uint32_t* __restrict__ ent) {
     const FitDev& f = *fp;
-    count_iteration(f, off, ent, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, f.n_qd,
-                    (int64_t)gridDim.x * blockDim.x, gridDim.x);
+    count_iteration<8>(f, off, ent, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, f.n_qd,
+                       (int64_t)gridDim.x * blockDim.x, gridDim.x);
 }
 
 cudaError_t launch_em_counts(const FitDev* fit, const uint32_t* off, const uint32_t* ent, int64_t n_qd, int n_sm,
@@ -389,7 +390,9 @@ cudaError_t launch_em_counts_pbm_dense(const FitDev* fit, const uint16_t* dense,
 
 // Many fits in one launch: fit i owns blocks [blk_begin, blk_begin + n_blocks),
 // each a contiguous chunk of kCountChunk of its qd, so a block serves one fit
-// and the fit's last block runs its public M-step.
+// and the fit's last block runs its public M-step.  (16 bin copies here, 8 in
+// the one-fit kernel: the batch's short-lived blocks gained from more copies,
+// the one-fit kernel's long grid-stride blocks lost occupancy to them.)
 __global__ void __launch_bounds__(256, 6) em_counts_batch_kernel(const CountFitDev* __restrict__ fits, int n_fits) {
     __shared__ int s_fit;
     if (threadIdx.x == 0) {
@@ -404,7 +407,7 @@ __global__ void __launch_bounds__(256, 6) em_counts_batch_kernel(const CountFitD
     const CountFitDev cf = fits[s_fit];
     const int64_t q0 = (int64_t)((int)blockIdx.x - cf.blk_begin) * kCountChunk;
     const int64_t q1 = q0 + kCountChunk < cf.n_qd ? q0 + kCountChunk : cf.n_qd;
-    count_iteration(*cf.fit, cf.off, cf.ent, q0 + threadIdx.x, q1, blockDim.x, (unsigned)cf.n_blocks);
+    count_iteration<16>(*cf.fit, cf.off, cf.ent, q0 + threadIdx.x, q1, blockDim.x, (unsigned)cf.n_blocks);
 }
 
 cudaError_t launch_em_counts_batch(const CountFitDev* fits, int n_fits, int total_blocks, cudaStream_t st) {
