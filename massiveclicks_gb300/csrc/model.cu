@@ -458,6 +458,16 @@ struct mc_model {
     }
     FitDev make_desc() const;
     int write_fit_desc();
+    // Every parameter at its prior value 1/2 (the default Param (1, 2), param.cuh:18-39)
+    // and the iteration counter at 0, queued on st.
+    int prior_values(cudaStream_t st) {
+        const std::vector<float> half(2 * MC_MAX_PUB, 0.5f);
+        CK(launch_fill_value(d_atr, qd_alloc(), 0.5f, st));
+        if (d_sat) CK(launch_fill_value(d_sat, qd_alloc(), 0.5f, st));
+        CK(cudaMemcpyAsync(d_pub_theta, half.data(), 2 * MC_MAX_PUB * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemsetAsync(d_iter, 0, 4, st));
+        return MC_OK;
+    }
     int ensure_plain(cudaStream_t st);
 };
 
@@ -1024,14 +1034,10 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
         pconst[(size_t)(2 * k)] = num;
         pconst[(size_t)(2 * k + 1)] = den;
     }
-    std::vector<float> half(2 * MC_MAX_PUB, 0.5f);
-    CK(launch_fill_value(m->d_atr, m->qd_alloc(), 0.5f, st));
-    if (m->d_sat) CK(launch_fill_value(m->d_sat, m->qd_alloc(), 0.5f, st));
-    CK(cudaMemcpyAsync(m->d_pub_theta, half.data(), 2 * MC_MAX_PUB * 4, cudaMemcpyHostToDevice, st));
+    if ((rc = m->prior_values(st))) return rc;
     CK(cudaMemsetAsync(m->d_pub_bins, 0, (size_t)(2 * m->n_pub) * 8, st));
     CK(cudaMemcpyAsync(m->d_pub_const, pconst.data(), pconst.size() * 8, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(m->d_tiles_done, 0, 4, st));
-    CK(cudaMemsetAsync(m->d_iter, 0, 4, st));
     CK(cudaMemsetAsync(m->d_status, 0, 4, st));
     CK(cudaMemsetAsync(m->d_ws, 0, sizeof(WorkState), st));
     CK(cudaStreamSynchronize(st));
@@ -1432,11 +1438,7 @@ extern "C" int mc_model_init_parameters(mc_model* m, void* stream) {
     if (!m->uploaded) return set_error(MC_ERR_STATE, "init_parameters: no training sessions uploaded");
     CK(cudaSetDevice(m->device));
     cudaStream_t st = m->pick(stream);
-    std::vector<float> half(2 * MC_MAX_PUB, 0.5f);
-    CK(launch_fill_value(m->d_atr, m->qd_alloc(), 0.5f, st));
-    if (m->d_sat) CK(launch_fill_value(m->d_sat, m->qd_alloc(), 0.5f, st));
-    CK(cudaMemcpyAsync(m->d_pub_theta, half.data(), 2 * MC_MAX_PUB * 4, cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(m->d_iter, 0, 4, st));
+    if (int rc = m->prior_values(st)) return rc;
     CK(cudaStreamSynchronize(st));
     return MC_OK;
 }
