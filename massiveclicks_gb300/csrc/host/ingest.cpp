@@ -28,13 +28,16 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <future>
 #include <iostream>
+#include <memory>
 #include <numeric>
 #include <string>
 #include <thread>
 #include <vector>
 
 #include "host_internal.h"
+#include "pool.h"
 
 namespace mch {
 
@@ -90,21 +93,22 @@ static void build_partition(const std::vector<int32_t>& query, const std::vector
     for (int64_t i = 0; i < n_train; i++) kv[(size_t)i] = {query[(size_t)i], (int32_t)i};
     std::sort(kv.begin(), kv.end(),
               [](const std::pair<int32_t, int32_t>& a, const std::pair<int32_t, int32_t>& b) { return a.first < b.first; });
-    std::vector<int32_t> order((size_t)n_train);
-    for (int64_t i = 0; i < n_train; i++) order[(size_t)i] = kv[(size_t)i].second;
-    std::vector<std::pair<int32_t, int32_t>>().swap(kv);
-
     SessionSet& tr = d->train;
     tr.query.resize((size_t)n_train);
     tr.docs.resize((size_t)n_train * MC_MAX_SERP);
     tr.pidx.assign((size_t)n_train * MC_MAX_SERP, -1);
     tr.click.resize((size_t)n_train);
-    for (int64_t i = 0; i < n_train; i++) {
-        int32_t src = order[(size_t)i];
-        tr.query[(size_t)i] = query[(size_t)src];
-        std::memcpy(&tr.docs[(size_t)i * MC_MAX_SERP], &docs[(size_t)src * MC_MAX_SERP], MC_MAX_SERP * sizeof(int32_t));
-        tr.click[(size_t)i] = click[(size_t)src];
-    }
+    const int64_t kGather = 65536;
+    parallel_for((size_t)((n_train + kGather - 1) / kGather), [&](size_t c) {
+        const int64_t i1 = std::min<int64_t>(n_train, (int64_t)(c + 1) * kGather);
+        for (int64_t i = (int64_t)c * kGather; i < i1; i++) {
+            const int32_t src = kv[(size_t)i].second;
+            tr.query[(size_t)i] = query[(size_t)src];
+            std::memcpy(&tr.docs[(size_t)i * MC_MAX_SERP], &docs[(size_t)src * MC_MAX_SERP], MC_MAX_SERP * sizeof(int32_t));
+            tr.click[(size_t)i] = click[(size_t)src];
+        }
+    });
+    std::vector<std::pair<int32_t, int32_t>>().swap(kv);
 
     // Query segments of the sorted training set.
     std::vector<int64_t> seg_begin;
@@ -114,73 +118,60 @@ static void build_partition(const std::vector<int32_t>& query, const std::vector
     seg_begin.push_back(n_train);
 
     // Per segment: distinct docs in order of first appearance get local
-    // indices 0..k-1; the lookup table keeps (doc, local index) sorted by doc.
+    // indices 0..k-1 (one scan with an open-addressing table of doc -> local
+    // index); the lookup table keeps (doc, local index) sorted by doc.
     std::vector<int64_t> seg_ndocs(n_seg, 0);
     std::vector<std::vector<std::pair<int32_t, int32_t>>> seg_lookup(n_seg);
     struct Scratch {
-        std::vector<uint64_t> keys;
-        std::vector<std::pair<uint32_t, uint32_t>> firsts;
-        std::vector<uint32_t> by_first;
-        std::vector<int32_t> local;
+        std::vector<int32_t> slot_doc, slot_local;  // slot_local -1 = empty
     };
     auto index_segment = [&](size_t s, Scratch& sc) {
-        int64_t b = seg_begin[s], e = seg_begin[s + 1];
-        size_t m = (size_t)(e - b) * MC_MAX_SERP;
-        std::vector<uint64_t>& keys = sc.keys;
-        keys.resize(m);
-        for (size_t k = 0; k < m; k++) {
-            uint32_t doc = (uint32_t)tr.docs[(size_t)b * MC_MAX_SERP + k];
-            keys[k] = ((uint64_t)(doc ^ 0x80000000u) << 32) | (uint64_t)k;  // signed doc order
+        const int64_t b = seg_begin[s], e = seg_begin[s + 1];
+        const size_t m = (size_t)(e - b) * MC_MAX_SERP;
+        size_t cap = 16;
+        while (cap < 2 * m) cap <<= 1;
+        if (sc.slot_doc.size() < cap) {
+            sc.slot_doc.resize(cap);
+            sc.slot_local.resize(cap);
         }
-        std::sort(keys.begin(), keys.end());
-        // Groups of equal doc: first element carries the first appearance.
-        std::vector<std::pair<uint32_t, uint32_t>>& firsts = sc.firsts;  // (first position, group start)
-        firsts.clear();
-        for (size_t k = 0; k < m; k++)
-            if (k == 0 || (keys[k] >> 32) != (keys[k - 1] >> 32)) firsts.push_back({(uint32_t)(keys[k] & 0xffffffffu), (uint32_t)k});
-        std::vector<uint32_t>& by_first = sc.by_first;
-        by_first.resize(firsts.size());
-        std::iota(by_first.begin(), by_first.end(), 0);
-        std::sort(by_first.begin(), by_first.end(), [&](uint32_t x, uint32_t y) { return firsts[x].first < firsts[y].first; });
-        std::vector<int32_t>& local = sc.local;
-        local.resize(firsts.size());
-        for (size_t r = 0; r < by_first.size(); r++) local[by_first[r]] = (int32_t)r;
+        std::fill(sc.slot_local.begin(), sc.slot_local.begin() + (long)cap, -1);
+        const uint32_t mask = (uint32_t)cap - 1;
         auto& lk = seg_lookup[s];
-        lk.resize(firsts.size());
-        for (size_t g = 0; g < firsts.size(); g++) {
-            size_t k0 = firsts[g].second, k1 = (g + 1 < firsts.size()) ? firsts[g + 1].second : m;
-            int32_t doc = (int32_t)((uint32_t)(keys[k0] >> 32) ^ 0x80000000u);
-            lk[g] = {doc, local[g]};
-            for (size_t k = k0; k < k1; k++)
-                tr.pidx[(size_t)b * MC_MAX_SERP + (keys[k] & 0xffffffffu)] = local[g];
+        lk.clear();
+        int32_t* const pidx = &tr.pidx[(size_t)b * MC_MAX_SERP];
+        const int32_t* const dk = &tr.docs[(size_t)b * MC_MAX_SERP];
+        for (size_t k = 0; k < m; k++) {
+            const int32_t doc = dk[k];
+            uint32_t h = ((uint32_t)doc * 0x9E3779B1u) & mask;
+            while (sc.slot_local[h] >= 0 && sc.slot_doc[h] != doc) h = (h + 1) & mask;
+            if (sc.slot_local[h] < 0) {
+                sc.slot_doc[h] = doc;
+                sc.slot_local[h] = (int32_t)lk.size();
+                lk.push_back({doc, (int32_t)lk.size()});
+            }
+            pidx[k] = sc.slot_local[h];
         }
-        seg_ndocs[s] = (int64_t)firsts.size();
+        seg_ndocs[s] = (int64_t)lk.size();
+        std::sort(lk.begin(), lk.end());
     };
-    unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    size_t n_threads = std::min<size_t>(hw, std::max<size_t>(1, n_seg / 64));
-    {
-        std::vector<std::thread> pool;
-        for (size_t t = 0; t < n_threads; t++)
-            pool.emplace_back([&, t]() {
-                Scratch sc;
-                for (size_t s = t; s < n_seg; s += n_threads) index_segment(s, sc);
-            });
-        for (auto& th : pool) th.join();
-    }
+    // Segments in tasks of 64, taken dynamically: one head query can hold a
+    // large share of all sessions.
+    const size_t kSegTask = 64;
+    parallel_for((n_seg + kSegTask - 1) / kSegTask, [&](size_t c) {
+        Scratch sc;  // per task: its tables grow to the task's largest segment
+        const size_t s1 = std::min(n_seg, (c + 1) * kSegTask);
+        for (size_t s = c * kSegTask; s < s1; s++) index_segment(s, sc);
+    });
     std::vector<int64_t> seg_base(n_seg + 1, 0);
     for (size_t s = 0; s < n_seg; s++) seg_base[s + 1] = seg_base[s] + seg_ndocs[s];
-    {
-        std::vector<std::thread> pool;
-        for (size_t t = 0; t < n_threads; t++)
-            pool.emplace_back([&, t]() {
-                for (size_t s = t; s < n_seg; s += n_threads) {
-                    int32_t base = (int32_t)seg_base[s];
-                    for (int64_t k = seg_begin[s] * MC_MAX_SERP; k < seg_begin[s + 1] * MC_MAX_SERP; k++)
-                        tr.pidx[(size_t)k] += base;
-                }
-            });
-        for (auto& th : pool) th.join();
-    }
+    parallel_for((n_seg + kSegTask - 1) / kSegTask, [&](size_t c) {
+        const size_t s1 = std::min(n_seg, (c + 1) * kSegTask);
+        for (size_t s = c * kSegTask; s < s1; s++) {
+            const int32_t base = (int32_t)seg_base[s];
+            for (int64_t k = seg_begin[s] * MC_MAX_SERP; k < seg_begin[s + 1] * MC_MAX_SERP; k++)
+                tr.pidx[(size_t)k] += base;
+        }
+    });
     d->n_qd = seg_base[n_seg];
 
     // Test set: the tail in arrival order, filtered; contiguous ranges on
@@ -212,16 +203,13 @@ static void build_partition(const std::vector<int32_t>& query, const std::vector
             out.click.push_back(click[(size_t)i]);
         }
     };
-    const int64_t n_tparts = std::max<int64_t>(1, std::min<int64_t>(hw, n_test / 65536));
+    const int64_t kTestPart = 16384;
+    const int64_t n_tparts = std::max<int64_t>(1, (n_test + kTestPart - 1) / kTestPart);
     std::vector<SessionSet> tparts((size_t)n_tparts);
-    {
-        std::vector<std::thread> pool;
-        for (int64_t t = 0; t < n_tparts; t++)
-            pool.emplace_back([&, t]() {
-                filter_range(n_train + n_test * t / n_tparts, n_train + n_test * (t + 1) / n_tparts, tparts[(size_t)t]);
-            });
-        for (auto& th : pool) th.join();
-    }
+    parallel_for((size_t)n_tparts, [&](size_t t) {
+        filter_range(n_train + (int64_t)t * kTestPart, std::min<int64_t>(n, n_train + ((int64_t)t + 1) * kTestPart),
+                     tparts[t]);
+    });
     SessionSet& te = d->test;
     for (const SessionSet& part : tparts) {
         te.query.insert(te.query.end(), part.query.begin(), part.query.end());
@@ -307,31 +295,57 @@ extern "C" int mc_dataset_parse(const char* path, int32_t max_sessions, float te
 
     const size_t kBlock = (size_t)64 << 20;
     const unsigned n_threads = std::max(1u, std::thread::hardware_concurrency());
-    std::vector<char> buf;
+    // Blocks are read into two buffers (left uninitialised: no zero fill of
+    // 64 MB per block): the next block is read on another thread while the
+    // current one is parsed and replayed.
+    struct Block {
+        std::unique_ptr<char[]> data;
+        size_t cap = 0, size = 0;
+        bool eof = false;
+    };
+    Block blocks[2];
+    auto read_block = [&](Block& b, const std::string& carry) {
+        const size_t need = carry.size() + kBlock;
+        if (b.cap < need) {
+            b.data.reset(new char[need]);
+            b.cap = need;
+        }
+        std::memcpy(b.data.get(), carry.data(), carry.size());
+        const size_t got = std::fread(b.data.get() + carry.size(), 1, kBlock, f);
+        b.size = carry.size() + got;
+        b.eof = got < kBlock;
+    };
     std::string carry;  // the unfinished last line of the previous block
     std::vector<std::vector<ParsedLine>> parts(n_threads);
+    int cur_b = 0;
+    read_block(blocks[0], carry);
+    std::future<void> pending;
     bool eof = false;
     while (!done && !eof) {
-        buf.assign(carry.begin(), carry.end());
-        const size_t have = buf.size();
-        buf.resize(have + kBlock);
-        const size_t got = std::fread(buf.data() + have, 1, kBlock, f);
-        buf.resize(have + got);
-        eof = got < kBlock;
+        if (pending.valid()) pending.get();  // blocks[cur_b] is read
+        Block& blk = blocks[cur_b];
+        eof = blk.eof;
+        const char* const bufp = blk.data.get();
         // Complete lines of this block: up to the last newline (all of it at EOF).
-        size_t end = buf.size();
+        size_t end = blk.size;
         if (!eof) {
             size_t nl = end;
-            while (nl > 0 && buf[nl - 1] != '\n') nl--;
+            while (nl > 0 && bufp[nl - 1] != '\n') nl--;
             if (nl == 0) {  // a line longer than the block: keep reading
-                carry.assign(buf.begin(), buf.end());
+                carry.assign(bufp, bufp + blk.size);
+                read_block(blk, carry);
                 continue;
             }
             end = nl;
         }
-        carry.assign(buf.begin() + (long)end, buf.end());
+        carry.assign(bufp + end, bufp + blk.size);
+        if (!eof) {
+            Block& next = blocks[cur_b ^ 1];
+            const std::string next_carry = carry;
+            pending = std::async(std::launch::async, [&read_block, &next, next_carry]() { read_block(next, next_carry); });
+        }
         if (end == 0) break;
-        const char* base = buf.data();
+        const char* base = bufp;
         // Thread ranges start at line boundaries.
         std::vector<size_t> cut(n_threads + 1, end);
         cut[0] = 0;
@@ -352,10 +366,7 @@ extern "C" int mc_dataset_parse(const char* path, int32_t max_sessions, float te
                 p = q + 1;
             }
         };
-        std::vector<std::thread> pool;
-        for (unsigned t = 1; t < n_threads; t++) pool.emplace_back(work, t);
-        work(0);
-        for (auto& th : pool) th.join();
+        parallel_for(n_threads, [&](size_t t) { work((unsigned)t); });
         for (unsigned t = 0; t < n_threads && !done; t++) {
             for (const ParsedLine& pl : parts[t]) {
                 if (!(n_queries < max_sessions || max_sessions == -1)) { done = true; break; }
@@ -379,7 +390,9 @@ extern "C" int mc_dataset_parse(const char* path, int32_t max_sessions, float te
                 have_prev = true;
             }
         }
+        cur_b ^= 1;  // the next block (being read) becomes current
     }
+    if (pending.valid()) pending.get();  // a read still in flight when the session limit stopped us
     std::fclose(f);
     mc_dataset* d = new (std::nothrow) mc_dataset();
     if (!d) return set_error(MC_ERR_NOMEM, "dataset_parse: out of host memory");
