@@ -418,7 +418,7 @@ def run_ours(args, rank: int, world: int, local: int):
         e2e_step()  # warm-up
         torch.cuda.synchronize()
         dist.barrier()
-        e2e_steps = 2
+        e2e_steps = 5
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
             e2e_step()
