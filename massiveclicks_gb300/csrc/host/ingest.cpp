@@ -267,6 +267,75 @@ static ParsedLine parse_line(const char* b, const char* e) {
     return pl;
 }
 
+// One contiguous run of lines replayed on its own.  Everything a line needs
+// from the lines before the run -- the open session and the last session id
+// -- is recorded at the run's boundary and settled when the runs are joined
+// in order (join_part); the sessions the run both opens and closes are
+// complete here.
+struct PartReplay {
+    int64_t n_lines = 0;
+    // Before the first query line: click docs for the incoming open session,
+    // and the session id of the last non-rejected line, if any.
+    std::vector<int32_t> prefix_clicks;
+    bool prefix_sid = false;
+    int32_t prefix_last_sid = 0;
+    int64_t first_query = -1;  // line index of the first query line, -1 if none
+    // Sessions opened and closed in the run, in order, and the index of the
+    // query line that closed each (a query line closes the open session when
+    // the previous non-rejected line's session id is not -1).
+    std::vector<int32_t> q, d;
+    std::vector<uint16_t> c;
+    std::vector<int64_t> closed_at;
+    RawSession open;               // opened by the last query line
+    bool any_sid = false;          // a non-rejected line in the run
+    int32_t last_sid = 0;          // the last one's session id
+    std::vector<std::pair<int64_t, std::string>> invalid;  // reported lines
+};
+
+static void replay_part(const char* base, size_t p, size_t e, PartReplay& out) {
+    out = PartReplay();
+    bool seen_query = false;
+    RawSession cur;
+    int64_t li = 0;
+    while (p < e) {
+        const char* nl = static_cast<const char*>(std::memchr(base + p, '\n', e - p));
+        const size_t q = nl ? (size_t)(nl - base) : e;
+        const ParsedLine pl = parse_line(base + p, base + q);
+        if (pl.kind == 0 || pl.kind == 3) out.invalid.push_back({li, std::string(pl.b, pl.e)});
+        if (pl.kind != 0) {
+            if (pl.kind == 1) {
+                if (!seen_query) {
+                    out.first_query = li;  // whether it closes the incoming session is settled at the join
+                    seen_query = true;
+                } else if (out.last_sid != -1) {
+                    out.q.push_back(cur.query);
+                    out.d.insert(out.d.end(), cur.docs, cur.docs + MC_MAX_SERP);
+                    out.c.push_back(cur.click);
+                    out.closed_at.push_back(li);
+                }
+                cur = RawSession();
+                cur.query = pl.query;
+                std::memcpy(cur.docs, pl.v, sizeof(cur.docs));
+            } else if (pl.kind == 2) {
+                if (!seen_query) out.prefix_clicks.push_back(pl.v[0]);
+                else
+                    for (int r = 0; r < MC_MAX_SERP; r++)
+                        if (cur.docs[r] == pl.v[0]) { cur.click |= (uint16_t)(1u << r); break; }
+            }
+            if (!seen_query) {
+                out.prefix_sid = true;
+                out.prefix_last_sid = pl.sid;
+            }
+            out.any_sid = true;
+            out.last_sid = pl.sid;
+        }
+        li++;
+        p = q + 1;
+    }
+    out.open = cur;
+    out.n_lines = li;
+}
+
 }  // namespace mch
 
 using namespace mch;
@@ -316,7 +385,61 @@ extern "C" int mc_dataset_parse(const char* path, int32_t max_sessions, float te
         b.eof = got < kBlock;
     };
     std::string carry;  // the unfinished last line of the previous block
-    std::vector<std::vector<ParsedLine>> parts(n_threads);
+    std::vector<PartReplay> parts(n_threads);
+    // Joins a replayed run to the state of the lines before it, in order: the
+    // session count is checked before every line (it changes only at query
+    // lines, so the stop falls on the line after the closing query line that
+    // reached the limit), reported lines are printed up to the stop, and the
+    // run's boundary facts are applied to the open session.
+    const auto limit_reached = [&]() { return !(n_queries < max_sessions || max_sessions == -1); };
+    auto push = [&](int32_t q, const int32_t* dd, uint16_t c) {
+        query.push_back(q);
+        docs.insert(docs.end(), dd, dd + MC_MAX_SERP);
+        click.push_back(c);
+        n_queries++;
+    };
+    auto report = [&](const PartReplay& P, int64_t upto) {  // lines with index < upto
+        for (const auto& m : P.invalid)
+            if (m.first < upto) std::cout << "\nInvalid data: " << m.second << std::endl;
+    };
+    auto join_part = [&](const PartReplay& P) {
+        if (P.n_lines == 0) return;
+        if (limit_reached()) { done = true; return; }  // stops before the run's first line
+        // The prefix: clicks on the incoming open session.
+        for (int32_t doc : P.prefix_clicks)
+            for (int r = 0; r < MC_MAX_SERP; r++)
+                if (cur.docs[r] == doc) { cur.click |= (uint16_t)(1u << r); break; }
+        if (P.prefix_sid) {
+            session_prev = P.prefix_last_sid;
+            have_prev = true;
+        }
+        if (P.first_query < 0) {  // no query line: the prefix is the whole run
+            report(P, P.n_lines);
+            return;
+        }
+        // The first query line closes the incoming session, then the run's own.
+        if (have_prev && session_prev != -1) {
+            push(cur.query, cur.docs, cur.click);
+            if (limit_reached() && P.first_query + 1 < P.n_lines) {
+                report(P, P.first_query + 1);
+                done = true;
+                return;
+            }
+        }
+        const size_t n_closed = P.closed_at.size();
+        for (size_t k = 0; k < n_closed; k++) {
+            push(P.q[k], &P.d[k * MC_MAX_SERP], P.c[k]);
+            if (limit_reached() && P.closed_at[k] + 1 < P.n_lines) {
+                report(P, P.closed_at[k] + 1);
+                done = true;
+                return;
+            }
+        }
+        report(P, P.n_lines);
+        cur = P.open;
+        session_prev = P.last_sid;
+        have_prev = true;
+    };
     int cur_b = 0;
     read_block(blocks[0], carry);
     std::future<void> pending;
@@ -354,42 +477,8 @@ extern "C" int mc_dataset_parse(const char* path, int32_t max_sessions, float te
             while (c < end && c > 0 && base[c - 1] != '\n') c++;
             cut[t] = c;
         }
-        auto work = [&](unsigned t) {
-            std::vector<ParsedLine>& v = parts[t];
-            v.clear();
-            size_t p = cut[t];
-            const size_t e = cut[t + 1];
-            while (p < e) {
-                const char* nl = static_cast<const char*>(std::memchr(base + p, '\n', e - p));
-                const size_t q = nl ? (size_t)(nl - base) : e;
-                v.push_back(parse_line(base + p, base + q));
-                p = q + 1;
-            }
-        };
-        parallel_for(n_threads, [&](size_t t) { work((unsigned)t); });
-        for (unsigned t = 0; t < n_threads && !done; t++) {
-            for (const ParsedLine& pl : parts[t]) {
-                if (!(n_queries < max_sessions || max_sessions == -1)) { done = true; break; }
-                if (pl.kind == 0 || pl.kind == 3) std::cout << "\nInvalid data: " << std::string(pl.b, pl.e) << std::endl;
-                if (pl.kind == 0) continue;
-                if (pl.kind == 1) {
-                    if (have_prev && session_prev != -1) {
-                        query.push_back(cur.query);
-                        docs.insert(docs.end(), cur.docs, cur.docs + MC_MAX_SERP);
-                        click.push_back(cur.click);
-                        n_queries++;
-                    }
-                    cur = RawSession();
-                    cur.query = pl.query;
-                    std::memcpy(cur.docs, pl.v, sizeof(cur.docs));
-                } else if (pl.kind == 2) {
-                    for (int r = 0; r < MC_MAX_SERP; r++)
-                        if (cur.docs[r] == pl.v[0]) { cur.click |= (uint16_t)(1u << r); break; }
-                }
-                session_prev = pl.sid;
-                have_prev = true;
-            }
-        }
+        parallel_for(n_threads, [&](size_t t) { replay_part(base, cut[t], cut[t + 1], parts[t]); });
+        for (unsigned t = 0; t < n_threads && !done; t++) join_part(parts[t]);
         cur_b ^= 1;  // the next block (being read) becomes current
     }
     if (pending.valid()) pending.get();  // a read still in flight when the session limit stopped us

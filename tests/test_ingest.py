@@ -115,3 +115,55 @@ def test_max_sessions_limits_reading(native_lib):
         api.write_log(cfg, str(log))
         ds = api.Dataset.parse(str(log), 100, 0.2)
     assert len(ds.train) == 80
+
+
+def _messy_log(seed: int, n_lines: int) -> str:
+    """Valid query and click lines mixed with every kind of line the reader
+    treats specially: session id -1, wrong token counts, unparsable session
+    ids and fields, empty lines, and click lines before the first query."""
+    rng = np.random.default_rng(seed)
+    lines = [f"{rng.integers(0, 50)} 1 C {rng.integers(0, 5)}" for _ in range(int(rng.integers(0, 3)))]
+    sid = 0
+    while len(lines) < n_lines:
+        u = rng.random()
+        if u < 0.55:
+            q = int(rng.zipf(1.5)) % 40
+            docs = rng.permutation(12)[:10] + q * 10
+            s = -1 if rng.random() < 0.05 else sid
+            lines.append(f"{s} 0 Q {q} 0 " + " ".join(str(int(d)) for d in docs))
+            for k in range(int(rng.integers(0, 3))):
+                lines.append(f"{s} {k + 1} C {int(rng.choice(docs)) if rng.random() < 0.9 else 999}")
+            sid += 1
+        elif u < 0.62:
+            lines.append("1 2 3 4 5")                                 # other token count
+        elif u < 0.67:
+            lines.append("x 0 Q 1 0 1 2 3 4 5 6 7 8 9 10")           # bad session id
+        elif u < 0.72:
+            lines.append(f"{sid} 0 Q 3 0 1 2 3 4 y 6 7 8 9 10")     # bad doc field
+        elif u < 0.76:
+            lines.append(f"{sid} 1 C zz")                             # bad click doc
+        elif u < 0.80:
+            lines.append("")                                          # empty line
+        elif u < 0.85:
+            lines.append(f"-1 1 C {int(rng.integers(0, 400))}")       # click line with session id -1
+        else:
+            lines.append(f"{sid} 1 C {int(rng.integers(0, 400))}")   # stray click
+    return "\n".join(lines) + "\n"
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+@pytest.mark.parametrize("max_sessions", [-1, 0, 1, 37, 400, 100000])
+def test_messy_log_matches_oracle_ingest(seed, max_sessions, native_lib, oracle_lib, capsys):
+    """Runs of lines are replayed on several threads and joined in order; the
+    result must be the oracle's line-by-line state machine, whatever mix of
+    malformed lines and wherever the session limit falls."""
+    from oracle import bindings
+    with tempfile.TemporaryDirectory() as tmp:
+        log = Path(tmp) / "log.txt"
+        log.write_text(_messy_log(seed, 4000))
+        ds = api.Dataset.parse(str(log), max_sessions, 0.2)
+        part = bindings.parse(str(log), max_sessions, 0.2)
+    assert ds.n_qd == part["n_qd"]
+    for s, st in (("train", ds.train), ("test", ds.test)):
+        for k in ("query", "docs", "pidx", "click"):
+            assert np.array_equal(getattr(st, k), part[s][k]), (seed, max_sessions, s, k)
