@@ -1,4 +1,5 @@
 // The reference's C++ host API (include/mclicks_host.hpp) over the C-ABI.
+#include <charconv>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -12,6 +13,7 @@
 
 #include "mclicks_host.hpp"
 #include "host_internal.h"
+#include "pool.h"
 
 namespace mclicks {
 
@@ -269,17 +271,44 @@ void output_parameters(const std::string& file_path, const Partition& partition,
         // The reference writes this header, then writes the data from offset
         // 0 of the same file (MPI_File_write_at_all), which overwrites it: its
         // files hold the data lines only, and so do these.
-        std::ofstream f(path);
+        // Lines are formatted on the host threads in chunks of sessions,
+        // a bounded group of chunks at a time, and written in order.
+        // std::to_chars (fixed, 6 digits; decimal for the ids) gives the text
+        // of std::to_string, which the reference writes.
+        std::ofstream f(path, std::ios::binary);
         const std::vector<Param>& v = *params.second[k];
-        std::string data;
-        for (const SERP_Hst& s : std::get<0>(partition)) {
-            for (int r = 0; r < MAX_SERP; r++) {
-                SearchResult_Hst sr = s[r];
-                float val = sr.get_param_index() != -1 ? v[(size_t)sr.get_param_index()].value() : 0.5f;
-                data += std::to_string(s.get_query()) + ", " + std::to_string(sr.get_doc_id()) + ", " + std::to_string(val) + "\n";
-            }
+        const TrainSet& train = std::get<0>(partition);
+        const size_t kChunk = 65536;
+        const size_t n_chunks = (train.size() + kChunk - 1) / kChunk;
+        const size_t group = 4 * mch::pool_threads();
+        std::vector<std::string> text(group);
+        for (size_t g0 = 0; g0 < n_chunks; g0 += group) {
+            const size_t g1 = std::min(n_chunks, g0 + group);
+            mch::parallel_for(g1 - g0, [&](size_t j) {
+                std::string& out = text[j];
+                out.clear();
+                const size_t s0 = (g0 + j) * kChunk, s1 = std::min(train.size(), s0 + kChunk);
+                out.reserve((s1 - s0) * MAX_SERP * 28);
+                char line[96];
+                for (size_t si = s0; si < s1; si++) {
+                    const SERP_Hst& sess = train[si];
+                    for (int r = 0; r < MAX_SERP; r++) {
+                        const SearchResult_Hst sr = sess[r];
+                        const float val = sr.get_param_index() != -1 ? v[(size_t)sr.get_param_index()].value() : 0.5f;
+                        char* p = std::to_chars(line, line + sizeof line, sess.get_query()).ptr;
+                        *p++ = ',';
+                        *p++ = ' ';
+                        p = std::to_chars(p, line + sizeof line, sr.get_doc_id()).ptr;
+                        *p++ = ',';
+                        *p++ = ' ';
+                        p = std::to_chars(p, line + sizeof line, val, std::chars_format::fixed, 6).ptr;
+                        *p++ = '\n';
+                        out.append(line, (size_t)(p - line));
+                    }
+                }
+            });
+            for (size_t j = 0; j < g1 - g0; j++) f.write(text[j].data(), (std::streamsize)text[j].size());
         }
-        f << data;
     }
 }
 
