@@ -77,10 +77,10 @@ static int64_t train_count(int64_t n, float test_share) {
     return n_train;
 }
 
-// Builds the partition from sessions in arrival order.
-static void build_partition(const std::vector<int32_t>& query, const std::vector<int32_t>& docs,
-                            const std::vector<uint16_t>& click, float test_share, mc_dataset* d) {
-    int64_t n = (int64_t)query.size();
+// Builds the partition from n sessions in arrival order (query[n],
+// docs[n * 10], click[n]).
+static void build_partition(int64_t n, const int32_t* query, const int32_t* docs, const uint16_t* click,
+                            float test_share, mc_dataset* d) {
     int64_t n_train = train_count(n, test_share);
     int64_t n_test = n - n_train;
 
@@ -89,26 +89,32 @@ static void build_partition(const std::vector<int32_t>& query, const std::vector
     // then makes the same comparisons with the same outcomes and the same
     // moves as on the sessions themselves, so it leaves the indices in the
     // reference's (unstable) order, without a random load per comparison.
-    std::vector<std::pair<int32_t, int32_t>> kv((size_t)n_train);
-    for (int64_t i = 0; i < n_train; i++) kv[(size_t)i] = {query[(size_t)i], (int32_t)i};
-    std::sort(kv.begin(), kv.end(),
-              [](const std::pair<int32_t, int32_t>& a, const std::pair<int32_t, int32_t>& b) { return a.first < b.first; });
+    struct KV {
+        int32_t first, second;  // query, session index
+    };
+    RawVec<KV> kv((size_t)n_train);
+    const int64_t kFill = 1 << 20;
+    parallel_for((size_t)((n_train + kFill - 1) / kFill), [&](size_t c) {
+        const int64_t i1 = std::min<int64_t>(n_train, (int64_t)(c + 1) * kFill);
+        for (int64_t i = (int64_t)c * kFill; i < i1; i++) kv[(size_t)i] = KV{query[i], (int32_t)i};
+    });
+    std::sort(kv.begin(), kv.end(), [](const KV& a, const KV& b) { return a.first < b.first; });
     SessionSet& tr = d->train;
     tr.query.resize((size_t)n_train);
     tr.docs.resize((size_t)n_train * MC_MAX_SERP);
-    tr.pidx.assign((size_t)n_train * MC_MAX_SERP, -1);
+    tr.pidx.resize((size_t)n_train * MC_MAX_SERP);  // every entry is written by the indexing below
     tr.click.resize((size_t)n_train);
     const int64_t kGather = 65536;
     parallel_for((size_t)((n_train + kGather - 1) / kGather), [&](size_t c) {
         const int64_t i1 = std::min<int64_t>(n_train, (int64_t)(c + 1) * kGather);
         for (int64_t i = (int64_t)c * kGather; i < i1; i++) {
-            const int32_t src = kv[(size_t)i].second;
-            tr.query[(size_t)i] = query[(size_t)src];
-            std::memcpy(&tr.docs[(size_t)i * MC_MAX_SERP], &docs[(size_t)src * MC_MAX_SERP], MC_MAX_SERP * sizeof(int32_t));
-            tr.click[(size_t)i] = click[(size_t)src];
+            const int64_t src = kv[(size_t)i].second;
+            tr.query[(size_t)i] = query[src];
+            std::memcpy(&tr.docs[(size_t)i * MC_MAX_SERP], &docs[src * MC_MAX_SERP], MC_MAX_SERP * sizeof(int32_t));
+            tr.click[(size_t)i] = click[src];
         }
     });
-    std::vector<std::pair<int32_t, int32_t>>().swap(kv);
+    RawVec<KV>().swap(kv);
 
     // Query segments of the sorted training set.
     std::vector<int64_t> seg_begin;
@@ -175,21 +181,24 @@ static void build_partition(const std::vector<int32_t>& query, const std::vector
     d->n_qd = seg_base[n_seg];
 
     // Test set: the tail in arrival order, filtered; contiguous ranges on
-    // several threads, joined in order.
+    // several threads, joined in order.  The segments' queries, in one small
+    // array, are binary-searched per test session.
+    std::vector<int32_t> seg_query(n_seg);
+    for (size_t g = 0; g < n_seg; g++) seg_query[g] = tr.query[(size_t)seg_begin[g]];
     auto filter_range = [&](int64_t i0, int64_t i1, SessionSet& out) {
+        out.query.reserve((size_t)(i1 - i0));
+        out.docs.reserve((size_t)(i1 - i0) * MC_MAX_SERP);
+        out.pidx.reserve((size_t)(i1 - i0) * MC_MAX_SERP);
+        out.click.reserve((size_t)(i1 - i0));
         for (int64_t i = i0; i < i1; i++) {
-            int32_t qi = query[(size_t)i];
-            size_t lo = 0, hi = n_seg;
-            while (lo < hi) {  // first segment with query >= qi
-                size_t mid = (lo + hi) / 2;
-                if (tr.query[(size_t)seg_begin[mid]] < qi) lo = mid + 1; else hi = mid;
-            }
-            if (lo == n_seg || tr.query[(size_t)seg_begin[lo]] != qi) continue;
+            const int32_t qi = query[i];
+            const size_t lo = (size_t)(std::lower_bound(seg_query.begin(), seg_query.end(), qi) - seg_query.begin());
+            if (lo == n_seg || seg_query[lo] != qi) continue;
             const auto& lk = seg_lookup[lo];
             int32_t p[MC_MAX_SERP];
             bool any = false;
             for (int r = 0; r < MC_MAX_SERP; r++) {
-                int32_t doc = docs[(size_t)i * MC_MAX_SERP + r];
+                int32_t doc = docs[i * MC_MAX_SERP + r];
                 auto it = std::lower_bound(lk.begin(), lk.end(), std::make_pair(doc, INT_MIN));
                 if (it != lk.end() && it->first == doc) { p[r] = (int32_t)seg_base[lo] + it->second; any = true; }
                 else p[r] = -1;
@@ -197,10 +206,10 @@ static void build_partition(const std::vector<int32_t>& query, const std::vector
             if (!any) continue;
             out.query.push_back(qi);
             for (int r = 0; r < MC_MAX_SERP; r++) {
-                out.docs.push_back(docs[(size_t)i * MC_MAX_SERP + r]);
+                out.docs.push_back(docs[i * MC_MAX_SERP + r]);
                 out.pidx.push_back(p[r]);
             }
-            out.click.push_back(click[(size_t)i]);
+            out.click.push_back(click[i]);
         }
     };
     const int64_t kTestPart = 16384;
@@ -211,12 +220,19 @@ static void build_partition(const std::vector<int32_t>& query, const std::vector
                      tparts[t]);
     });
     SessionSet& te = d->test;
-    for (const SessionSet& part : tparts) {
-        te.query.insert(te.query.end(), part.query.begin(), part.query.end());
-        te.docs.insert(te.docs.end(), part.docs.begin(), part.docs.end());
-        te.pidx.insert(te.pidx.end(), part.pidx.begin(), part.pidx.end());
-        te.click.insert(te.click.end(), part.click.begin(), part.click.end());
-    }
+    std::vector<size_t> at(tparts.size() + 1, 0);
+    for (size_t t = 0; t < tparts.size(); t++) at[t + 1] = at[t] + tparts[t].query.size();
+    te.query.resize(at.back());
+    te.docs.resize(at.back() * MC_MAX_SERP);
+    te.pidx.resize(at.back() * MC_MAX_SERP);
+    te.click.resize(at.back());
+    parallel_for(tparts.size(), [&](size_t t) {
+        const SessionSet& part = tparts[t];
+        std::copy(part.query.begin(), part.query.end(), te.query.begin() + (long)at[t]);
+        std::copy(part.docs.begin(), part.docs.end(), te.docs.begin() + (long)(at[t] * MC_MAX_SERP));
+        std::copy(part.pidx.begin(), part.pidx.end(), te.pidx.begin() + (long)(at[t] * MC_MAX_SERP));
+        std::copy(part.click.begin(), part.click.end(), te.click.begin() + (long)at[t]);
+    });
     (void)n_test;
 }
 
@@ -485,7 +501,7 @@ extern "C" int mc_dataset_parse(const char* path, int32_t max_sessions, float te
     std::fclose(f);
     mc_dataset* d = new (std::nothrow) mc_dataset();
     if (!d) return set_error(MC_ERR_NOMEM, "dataset_parse: out of host memory");
-    build_partition(query, docs, click, test_share, d);
+    build_partition((int64_t)query.size(), query.data(), docs.data(), click.data(), test_share, d);
     *out = d;
     return MC_OK;
 }
@@ -498,11 +514,9 @@ extern "C" int mc_dataset_from_sessions(int64_t n, const int32_t* query, const i
     if (n > 0 && (!query || !docs || !click_mask)) return set_error(MC_ERR_INVALID, "dataset_from_sessions: null input");
     if (!(test_share >= 0.0f && test_share <= 1.0f))
         return set_error(MC_ERR_INVALID, "dataset_from_sessions: test_share must be in [0, 1]");
-    std::vector<int32_t> q(query, query + n), dd(docs, docs + n * MC_MAX_SERP);
-    std::vector<uint16_t> c(click_mask, click_mask + n);
     mc_dataset* d = new (std::nothrow) mc_dataset();
     if (!d) return set_error(MC_ERR_NOMEM, "dataset_from_sessions: out of host memory");
-    build_partition(q, dd, c, test_share, d);
+    build_partition(n, query, docs, click_mask, test_share, d);  // reads the caller's arrays
     *out = d;
     return MC_OK;
 }
@@ -520,10 +534,16 @@ extern "C" int mc_dataset_copy(const mc_dataset* d, int which, int32_t* query, i
     if (!d) return set_error(MC_ERR_INVALID, "dataset_copy: null dataset");
     if (which != 0 && which != 1) return set_error(MC_ERR_INVALID, "dataset_copy: which must be 0 (train) or 1 (test)");
     const SessionSet& s = which == 0 ? d->train : d->test;
-    if (query) std::copy(s.query.begin(), s.query.end(), query);
-    if (docs) std::copy(s.docs.begin(), s.docs.end(), docs);
-    if (pidx) std::copy(s.pidx.begin(), s.pidx.end(), pidx);
-    if (click_mask) std::copy(s.click.begin(), s.click.end(), click_mask);
+    // In chunks on the host threads (the caller's fresh arrays are first
+    // touched in parallel too).
+    const int64_t n = s.size(), kCopy = 1 << 18;
+    parallel_for((size_t)((n + kCopy - 1) / kCopy), [&](size_t c) {
+        const int64_t i0 = (int64_t)c * kCopy, i1 = std::min<int64_t>(n, i0 + kCopy);
+        if (query) std::copy(s.query.begin() + i0, s.query.begin() + i1, query + i0);
+        if (docs) std::copy(s.docs.begin() + i0 * MC_MAX_SERP, s.docs.begin() + i1 * MC_MAX_SERP, docs + i0 * MC_MAX_SERP);
+        if (pidx) std::copy(s.pidx.begin() + i0 * MC_MAX_SERP, s.pidx.begin() + i1 * MC_MAX_SERP, pidx + i0 * MC_MAX_SERP);
+        if (click_mask) std::copy(s.click.begin() + i0, s.click.begin() + i1, click_mask + i0);
+    });
     return MC_OK;
 }
 
