@@ -134,23 +134,43 @@ static void build_partition(int64_t n, const int32_t* query, const int32_t* docs
     auto index_segment = [&](size_t s, Scratch& sc) {
         const int64_t b = seg_begin[s], e = seg_begin[s + 1];
         const size_t m = (size_t)(e - b) * MC_MAX_SERP;
-        size_t cap = 16;
-        while (cap < 2 * m) cap <<= 1;
-        if (sc.slot_doc.size() < cap) {
-            sc.slot_doc.resize(cap);
-            sc.slot_local.resize(cap);
-        }
-        std::fill(sc.slot_local.begin(), sc.slot_local.begin() + (long)cap, -1);
-        const uint32_t mask = (uint32_t)cap - 1;
+        // The table starts small and doubles when half full (rehashed from
+        // lk, which holds every (doc, local index) so far): a query's
+        // distinct docs are few even when its sessions are many.
+        size_t cap = 64;
+        auto clear_table = [&]() {
+            if (sc.slot_doc.size() < cap) {
+                sc.slot_doc.resize(cap);
+                sc.slot_local.resize(cap);
+            }
+            std::fill(sc.slot_local.begin(), sc.slot_local.begin() + (long)cap, -1);
+        };
+        clear_table();
+        uint32_t mask = (uint32_t)cap - 1;
         auto& lk = seg_lookup[s];
         lk.clear();
+        auto slot_of = [&](int32_t doc) {
+            uint32_t h = ((uint32_t)doc * 0x9E3779B1u) & mask;
+            while (sc.slot_local[h] >= 0 && sc.slot_doc[h] != doc) h = (h + 1) & mask;
+            return h;
+        };
         int32_t* const pidx = &tr.pidx[(size_t)b * MC_MAX_SERP];
         const int32_t* const dk = &tr.docs[(size_t)b * MC_MAX_SERP];
         for (size_t k = 0; k < m; k++) {
             const int32_t doc = dk[k];
-            uint32_t h = ((uint32_t)doc * 0x9E3779B1u) & mask;
-            while (sc.slot_local[h] >= 0 && sc.slot_doc[h] != doc) h = (h + 1) & mask;
+            uint32_t h = slot_of(doc);
             if (sc.slot_local[h] < 0) {
+                if (2 * (lk.size() + 1) > cap) {
+                    cap *= 2;
+                    mask = (uint32_t)cap - 1;
+                    clear_table();
+                    for (const auto& kv2 : lk) {
+                        const uint32_t h2 = slot_of(kv2.first);
+                        sc.slot_doc[h2] = kv2.first;
+                        sc.slot_local[h2] = kv2.second;
+                    }
+                    h = slot_of(doc);
+                }
                 sc.slot_doc[h] = doc;
                 sc.slot_local[h] = (int32_t)lk.size();
                 lk.push_back({doc, (int32_t)lk.size()});
@@ -370,8 +390,15 @@ extern "C" int mc_dataset_parse(const char* path, int32_t max_sessions, float te
     FILE* f = std::fopen(path, "rb");
     if (!f) return set_error(MC_ERR_IO, std::string("Unable to open the raw dataset: ") + path);
 
-    std::vector<int32_t> query, docs;
-    std::vector<uint16_t> click;
+    // Sessions kept, in order, as a list of chunks: a run's own sessions are
+    // moved in whole, boundary sessions appended one by one to a tail chunk;
+    // the chunks are concatenated once at the end.
+    struct Chunk {
+        std::vector<int32_t> q, d;
+        std::vector<uint16_t> c;
+        bool whole = false;  // a run's sessions (no appends)
+    };
+    std::vector<Chunk> chunks;
     RawSession cur;
     int64_t n_queries = 0;
     long long session_prev = -1;
@@ -409,16 +436,18 @@ extern "C" int mc_dataset_parse(const char* path, int32_t max_sessions, float te
     // run's boundary facts are applied to the open session.
     const auto limit_reached = [&]() { return !(n_queries < max_sessions || max_sessions == -1); };
     auto push = [&](int32_t q, const int32_t* dd, uint16_t c) {
-        query.push_back(q);
-        docs.insert(docs.end(), dd, dd + MC_MAX_SERP);
-        click.push_back(c);
+        if (chunks.empty() || chunks.back().whole) chunks.emplace_back();
+        Chunk& t = chunks.back();
+        t.q.push_back(q);
+        t.d.insert(t.d.end(), dd, dd + MC_MAX_SERP);
+        t.c.push_back(c);
         n_queries++;
     };
     auto report = [&](const PartReplay& P, int64_t upto) {  // lines with index < upto
         for (const auto& m : P.invalid)
             if (m.first < upto) std::cout << "\nInvalid data: " << m.second << std::endl;
     };
-    auto join_part = [&](const PartReplay& P) {
+    auto join_part = [&](PartReplay& P) {
         if (P.n_lines == 0) return;
         if (limit_reached()) { done = true; return; }  // stops before the run's first line
         // The prefix: clicks on the incoming open session.
@@ -443,7 +472,18 @@ extern "C" int mc_dataset_parse(const char* path, int32_t max_sessions, float te
             }
         }
         const size_t n_closed = P.closed_at.size();
-        for (size_t k = 0; k < n_closed; k++) {
+        if (max_sessions == -1 || n_queries + (int64_t)n_closed < (int64_t)max_sessions) {
+            // The limit cannot fall inside the run: its sessions in one move.
+            if (n_closed) {
+                chunks.emplace_back();
+                Chunk& t = chunks.back();
+                t.q = std::move(P.q);
+                t.d = std::move(P.d);
+                t.c = std::move(P.c);
+                t.whole = true;
+            }
+            n_queries += (int64_t)n_closed;
+        } else for (size_t k = 0; k < n_closed; k++) {
             push(P.q[k], &P.d[k * MC_MAX_SERP], P.c[k]);
             if (limit_reached() && P.closed_at[k] + 1 < P.n_lines) {
                 report(P, P.closed_at[k] + 1);
@@ -501,6 +541,17 @@ extern "C" int mc_dataset_parse(const char* path, int32_t max_sessions, float te
     std::fclose(f);
     mc_dataset* d = new (std::nothrow) mc_dataset();
     if (!d) return set_error(MC_ERR_NOMEM, "dataset_parse: out of host memory");
+    std::vector<size_t> at(chunks.size() + 1, 0);
+    for (size_t k = 0; k < chunks.size(); k++) at[k + 1] = at[k] + chunks[k].q.size();
+    RawVec<int32_t> query(at.back()), docs(at.back() * MC_MAX_SERP);
+    RawVec<uint16_t> click(at.back());
+    parallel_for(chunks.size(), [&](size_t k) {
+        const Chunk& t = chunks[k];
+        std::copy(t.q.begin(), t.q.end(), query.begin() + (long)at[k]);
+        std::copy(t.d.begin(), t.d.end(), docs.begin() + (long)(at[k] * MC_MAX_SERP));
+        std::copy(t.c.begin(), t.c.end(), click.begin() + (long)at[k]);
+    });
+    std::vector<Chunk>().swap(chunks);
     build_partition((int64_t)query.size(), query.data(), docs.data(), click.data(), test_share, d);
     *out = d;
     return MC_OK;
