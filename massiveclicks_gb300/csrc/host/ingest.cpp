@@ -268,7 +268,16 @@ struct ParsedLine {
     uint8_t kind;
 };
 
-static inline bool is_space(char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r'; }
+// The six characters std::isspace accepts in the "C" locale, as a table
+// indexed by the byte (one load per character instead of six compares).
+struct SpaceTable {
+    bool t[256] = {};
+    SpaceTable() {
+        for (unsigned char c : {' ', '\t', '\n', '\v', '\f', '\r'}) t[c] = true;
+    }
+};
+static const SpaceTable kSpace;
+static inline bool is_space(char c) { return kSpace.t[(unsigned char)c]; }
 
 // Tokens as the reference's std::istringstream >> splits them (whitespace).
 static ParsedLine parse_line(const char* b, const char* e) {
