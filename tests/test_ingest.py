@@ -153,7 +153,7 @@ def _messy_log(seed: int, n_lines: int) -> str:
 
 @pytest.mark.parametrize("seed", [1, 2, 3])
 @pytest.mark.parametrize("max_sessions", [-1, 0, 1, 37, 400, 100000])
-def test_messy_log_matches_oracle_ingest(seed, max_sessions, native_lib, oracle_lib, capsys):
+def test_messy_log_matches_oracle_ingest(seed, max_sessions, native_lib, oracle_lib):
     """Runs of lines are replayed on several threads and joined in order; the
     result must be the oracle's line-by-line state machine, whatever mix of
     malformed lines and wherever the session limit falls."""
