@@ -66,6 +66,9 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
+    ap.add_argument("--parity-iters", type=int, default=50,
+                    help="iterations of the fused GPU fit and the FP64 oracle on the CPU leg's sample "
+                         "(the bench line's error against the oracle; 0 skips)")
     ap.add_argument("--workload", choices=["dbn20m", "batched", "adjoint"], default="dbn20m",
                     help="dbn20m: the headline DBN fit; batched: 256 mixed fits in one launch; "
                          "adjoint: EM against the gradient trainer")
@@ -167,6 +170,60 @@ def time_cpu_oracle(ds, idx: np.ndarray, iters: int, warmup: int, threads: int, 
         fit.run(1, threads)
         times.append(time.perf_counter() - t0)
     return times
+
+
+def sample_sets(ds, idx: np.ndarray):
+    """The training sessions idx (whole queries) with their qd indices
+    renumbered densely in order, and the test sessions of the same queries with
+    the same renumbering (a test doc unseen in training stays -1)."""
+    from massiveclicks_gb300 import api
+    tr = ds.train
+    p = tr.pidx[idx]
+    used = np.unique(p)
+    remap = np.full(ds.n_qd + 1, -1, np.int64)        # slot n_qd maps -1 to -1
+    remap[used] = np.arange(len(used))
+    train = api.SessionSet(tr.query[idx], tr.docs[idx], remap[p].astype(np.int32), tr.click[idx])
+    te = ds.test
+    keep = np.isin(te.query, np.unique(tr.query[idx]))
+    tp = te.pidx[keep]
+    test = api.SessionSet(te.query[keep], te.docs[keep], remap[np.where(tp < 0, ds.n_qd, tp)].astype(np.int32),
+                          te.click[keep])
+    return train, test, int(len(used))
+
+
+def parity_vs_oracle(ds, idx: np.ndarray, model: int, iters: int, threads: int, stream, device: int) -> dict:
+    """The fused GPU fit and the FP64 oracle (the reference's CPU path in
+    double precision) on the same bounded sample, from the prior, for `iters`
+    iterations: parameter and test-set errors of the GPU against the oracle."""
+    from massiveclicks_gb300 import api
+    from massiveclicks_gb300._capi import IMPL_FUSED
+    from oracle import bindings
+    train, test, n_qd = sample_sets(ds, idx)
+    cm = api.ClickModel.create(model, device=device)
+    cm.upload(train, n_qd, stream)
+    cm.upload_test(test, stream)
+    cm.em(iters, IMPL_FUSED, stream)
+    ev = cm.evaluate(1, stream)
+    got = cm.get_parameters()
+    cm.destroy_parameters()
+    f = bindings.OracleFit("f64", model, 0, train.query, train.pidx, train.click, n_qd)
+    f.run(iters, threads=threads, copy_sessions=False)
+    ref = f.values()
+    ref_ev = f.evaluate(test.pidx, test.click)
+    worst_rel, worst_abs, worst_bar = 0.0, 0.0, 0.0
+    for k, r in ref.items():
+        err = np.abs(got[k].astype(np.float64) - r)
+        worst_abs = max(worst_abs, float(err.max()))
+        worst_rel = max(worst_rel, float((err / np.maximum(np.abs(r), 1e-30)).max()))
+        worst_bar = max(worst_bar, float((err / (1e-5 * np.abs(r) + 1e-6)).max()))
+    return {"against": "FP64 oracle (the reference's CPU path in double precision)", "iterations": iters,
+            "train_sessions": len(train), "test_sessions": len(test), "n_qd": n_qd,
+            "max_param_abs_err": worst_abs, "max_param_rel_err": worst_rel,
+            "max_param_err_over_bar": worst_bar, "param_bar": "1e-5 * |f64| + 1e-6",
+            "test_llh": ev.llh, "oracle_test_llh": ref_ev["llh"],
+            "test_llh_rel_err": abs(ev.llh - ref_ev["llh"]) / abs(ref_ev["llh"]),
+            "perplexity": ev.perplexity, "oracle_perplexity": ref_ev["ppl"],
+            "perplexity_rel_err": abs(ev.perplexity - ref_ev["ppl"]) / ref_ev["ppl"]}
 
 
 class ClockSampler:
@@ -438,6 +495,8 @@ def run_ours(args, rank: int, world: int, local: int):
         cpu = {"value": n * len(times) / sum(times), "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{n} training sessions (whole queries), {len(times)} iterations after 1 warm-up; "
                          "FP32 restatement of the reference's CPU path with its threading"}
+        if args.parity_iters > 0:
+            out["parity"] = parity_vs_oracle(ds, idx, MODELS[args.model], args.parity_iters, threads, stream, local)
 
     if rank == 0:
         line = {

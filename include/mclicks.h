@@ -101,6 +101,14 @@ typedef struct mc_dataset mc_dataset;
 
 int mc_dataset_parse(const char* path, int32_t max_sessions, float test_share, mc_dataset** out);
 
+/* How mc_dataset_parse reads a log (process-wide; no counterpart in the
+ * reference, which reads line by line with std::getline, dataset.cpp:224-305):
+ * block_bytes per read (default 64 MB) and the number of runs of lines each
+ * block is cut into and parsed in parallel (default one per hardware thread).
+ * 0 restores a default.  The output does not depend on either: small values
+ * make short logs cross many block and run boundaries, as a large log does. */
+int mc_ingest_configure(int64_t block_bytes, int32_t runs);
+
 /* Same split/sort/index steps on sessions already in memory, in arrival
  * order (as the parser would have produced them). */
 int mc_dataset_from_sessions(int64_t n, const int32_t* query, const int32_t* docs,

@@ -37,6 +37,7 @@ _SIGS = {
     "mc_synth_generate": (C.c_int, [C.POINTER(SynthConfig), _I64, _I64, _VP, _VP, _VP]),
     "mc_synth_write_log": (C.c_int, [C.POINTER(SynthConfig), C.c_char_p]),
     "mc_dataset_parse": (C.c_int, [C.c_char_p, _I32, _F32, C.POINTER(_VP)]),
+    "mc_ingest_configure": (C.c_int, [_I64, _I32]),
     "mc_dataset_from_sessions": (C.c_int, [_I64, _VP, _VP, _VP, _F32, C.POINTER(_VP)]),
     "mc_dataset_info": (C.c_int, [_VP, C.POINTER(_I64), C.POINTER(_I64), C.POINTER(_I64)]),
     "mc_dataset_copy": (C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP]),

@@ -22,6 +22,7 @@
 // (the reference keeps an uninitialised one); a split that would keep more
 // training sessions than exist keeps them all.
 #include <algorithm>
+#include <atomic>
 #include <cerrno>
 #include <climits>
 #include <cstdio>
@@ -385,6 +386,18 @@ static void replay_part(const char* base, size_t p, size_t e, PartReplay& out) {
 
 using namespace mch;
 
+// Read size and run count of mc_dataset_parse; 0 = the defaults (64 MB
+// blocks, one run of lines per hardware thread).
+static std::atomic<int64_t> g_block_bytes{0};
+static std::atomic<int32_t> g_parse_runs{0};
+
+extern "C" int mc_ingest_configure(int64_t block_bytes, int32_t runs) {
+    if (block_bytes < 0 || runs < 0) return set_error(MC_ERR_INVALID, "ingest_configure: negative size");
+    g_block_bytes.store(block_bytes);
+    g_parse_runs.store(runs);
+    return MC_OK;
+}
+
 // The text log is read in blocks; the lines of a block are parsed by several
 // threads (each a contiguous run of lines) and then replayed in order through
 // the reference's session state machine (dataset.cpp:224-305): the session
@@ -414,8 +427,9 @@ extern "C" int mc_dataset_parse(const char* path, int32_t max_sessions, float te
     bool have_prev = false;
     bool done = false;
 
-    const size_t kBlock = (size_t)64 << 20;
-    const unsigned n_threads = std::max(1u, std::thread::hardware_concurrency());
+    const size_t kBlock = g_block_bytes.load() > 0 ? (size_t)g_block_bytes.load() : (size_t)64 << 20;
+    const unsigned n_threads = g_parse_runs.load() > 0 ? (unsigned)g_parse_runs.load()
+                                                       : std::max(1u, std::thread::hardware_concurrency());
     // Blocks are read into two buffers (left uninitialised: no zero fill of
     // 64 MB per block): the next block is read on another thread while the
     // current one is parsed and replayed.

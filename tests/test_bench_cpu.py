@@ -39,3 +39,30 @@ def test_workload_text_follows_the_sizes():
     assert "250,000 sessions, 20,000 queries" in bench.data_text(b)
     assert bench.metric_for("dbn") != bench.metric_for("pbm")
     assert "PBM" in bench.metric_for("pbm")
+
+
+def test_sample_sets_renumber_densely(native_lib):
+    """The bench line's parity sample: whole queries, qd indices renumbered
+    densely and in order (so each query still owns a contiguous range), and
+    the test sessions of the sampled queries with the same renumbering."""
+    from massiveclicks_gb300 import api
+    cfg = api.synth_config(2, n_sessions=30_000, n_queries=3_000)
+    q, d, m = api.synth_sessions(cfg)
+    ds = api.Dataset.from_sessions(q, d, m, 0.2)
+    idx = bench.cpu_sample(ds, 5_000)
+    train, test, n_qd = bench.sample_sets(ds, idx)
+    for k in ("query", "docs", "click"):
+        assert np.array_equal(getattr(train, k), getattr(ds.train, k)[idx]), k
+    full = ds.train.pidx[idx].ravel()
+    mine = train.pidx.ravel()
+    assert np.array_equal(np.unique(mine), np.arange(n_qd))
+    order = np.argsort(full, kind="stable")
+    assert np.all(np.diff(mine[order]) >= 0)                 # the renumbering keeps the order
+    assert np.array_equal(np.diff(full[order]) == 0, np.diff(mine[order]) == 0)
+    sampled = np.unique(train.query)
+    keep = np.isin(ds.test.query, sampled)
+    assert len(test) == int(keep.sum())
+    assert np.array_equal(test.pidx < 0, ds.test.pidx[keep] < 0)
+    seen = ds.test.pidx[keep] >= 0
+    lut = dict(zip(full.tolist(), mine.tolist()))
+    assert all(lut[a] == b for a, b in zip(ds.test.pidx[keep][seen].tolist(), test.pidx[seen].tolist()))

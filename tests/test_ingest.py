@@ -167,3 +167,68 @@ def test_messy_log_matches_oracle_ingest(seed, max_sessions, native_lib, oracle_
     for s, st in (("train", ds.train), ("test", ds.test)):
         for k in ("query", "docs", "pidx", "click"):
             assert np.array_equal(getattr(st, k), part[s][k]), (seed, max_sessions, s, k)
+
+
+@pytest.fixture
+def small_blocks(native_lib):
+    """Reads with the given block size and run count, restoring the defaults
+    afterwards."""
+    def set_(block_bytes: int, runs: int):
+        _capi.check(native_lib.mc_ingest_configure(block_bytes, runs))
+    yield set_
+    _capi.check(native_lib.mc_ingest_configure(0, 0))
+
+
+@pytest.mark.parametrize("block_bytes,runs", [(40, 1), (333, 3), (4096, 7), (65536, 16)])
+@pytest.mark.parametrize("max_sessions", [-1, 37, 400])
+def test_messy_log_across_blocks(block_bytes, runs, max_sessions, small_blocks, oracle_lib):
+    """Blocks of a few bytes to a few KB put block boundaries inside lines
+    (the unfinished line is carried into the next block), lines longer than a
+    block (read on until a newline turns up), and sessions open across blocks
+    and runs, as a log of several hundred MB does with the default 64 MB
+    blocks."""
+    from oracle import bindings
+    small_blocks(block_bytes, runs)
+    with tempfile.TemporaryDirectory() as tmp:
+        log = Path(tmp) / "log.txt"
+        log.write_text(_messy_log(11, 3000))
+        ds = api.Dataset.parse(str(log), max_sessions, 0.2)
+        part = bindings.parse(str(log), max_sessions, 0.2)
+    assert ds.n_qd == part["n_qd"]
+    for s, st in (("train", ds.train), ("test", ds.test)):
+        for k in ("query", "docs", "pidx", "click"):
+            assert np.array_equal(getattr(st, k), part[s][k]), (block_bytes, runs, max_sessions, s, k)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_goldens_across_blocks(name, small_blocks):
+    """The reference's own partitions, read in 1 KB blocks cut into 5 runs."""
+    small_blocks(1024, 5)
+    case = load_case(name)
+    with tempfile.TemporaryDirectory() as tmp:
+        log = Path(tmp) / "log.txt"
+        log.write_bytes(case["log"].tobytes())
+        ds = api.Dataset.parse(str(log), int(case["max_sessions"]), float(case["test_share"]))
+    assert ds.n_qd == int(case["n_qd"])
+    for s, st in (("train", ds.train), ("test", ds.test)):
+        for k in ("query", "docs", "pidx", "click"):
+            assert np.array_equal(getattr(st, k), case[f"{s}_{k}"]), (name, s, k)
+
+
+def test_log_over_64mb_matches_oracle_ingest(native_lib, oracle_lib):
+    """A log larger than one default 64 MB block (about 900k sessions, 80 MB)
+    with the default block size and runs, against the oracle's line-by-line
+    reader; the session limit falls in the second block."""
+    from oracle import bindings
+    cfg = api.synth_config(1, n_sessions=900_000, n_queries=50_000)
+    with tempfile.TemporaryDirectory() as tmp:
+        log = Path(tmp) / "log.txt"
+        api.write_log(cfg, str(log))
+        assert log.stat().st_size > (64 << 20)
+        for limit in (-1, 850_000):
+            ds = api.Dataset.parse(str(log), limit, 0.2)
+            part = bindings.parse(str(log), limit, 0.2)
+            assert ds.n_qd == part["n_qd"]
+            for s, st in (("train", ds.train), ("test", ds.test)):
+                for k in ("query", "docs", "pidx", "click"):
+                    assert np.array_equal(getattr(st, k), part[s][k]), (limit, s, k)
