@@ -11,6 +11,9 @@
 #include <stdexcept>
 #include <string>
 
+#include <cuda_runtime.h>
+#include <unistd.h>
+
 #include "mclicks_host.hpp"
 #include "host_internal.h"
 #include "pool.h"
@@ -41,6 +44,21 @@ uint16_t SERP_Hst::click_mask() const {
     return m;
 }
 
+SERP_Hst::SERP_Hst(const std::vector<std::string>& line) {
+    query_ = std::stoi(line.at(3));
+    for (int r = 0; r < MAX_SERP; r++) session_[r] = SearchResult_Hst(std::stoi(line.at((size_t)r + 5)), 0, -1);
+}
+
+bool SERP_Hst::update_click_res(const std::vector<std::string>& line) {
+    const int doc = std::stoi(line.at(3));
+    for (int r = 0; r < MAX_SERP; r++)
+        if (session_[r].get_doc_id() == doc) {
+            session_[r].update_click(1);
+            return true;
+        }
+    return false;
+}
+
 static void to_serps(const mc_dataset* d, int which, std::vector<SERP_Hst>& out) {
     const mch::SessionSet& s = which == 0 ? d->train : d->test;
     out.resize((size_t)s.size());
@@ -53,7 +71,71 @@ static void to_serps(const mc_dataset* d, int which, std::vector<SERP_Hst>& out)
     }
 }
 
+ClusterProperties local_cluster_properties(const ProcessingConfig& config) {
+    ClusterProperties c;
+    NodeProperties node;
+    node.host.node_id = config.node_id;
+    node.host.thread_count = config.thread_count;
+    if (config.host_name[0]) std::snprintf(node.host.host_name, HOST_NAME_MAX, "%s", config.host_name);
+    else if (gethostname(node.host.host_name, HOST_NAME_MAX) != 0) node.host.host_name[0] = 0;
+    node.host.host_name[HOST_NAME_MAX - 1] = 0;
+    const long pages = sysconf(_SC_PHYS_PAGES), avail = sysconf(_SC_AVPHYS_PAGES), psize = sysconf(_SC_PAGE_SIZE);
+    if (pages > 0 && psize > 0) node.host.total_memory = (size_t)pages * (size_t)psize;
+    if (avail > 0 && psize > 0) node.host.free_memory = (size_t)avail * (size_t)psize;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    for (int d = 0; d < n; d++) {
+        cudaDeviceProp p;
+        if (cudaGetDeviceProperties(&p, d) != cudaSuccess) continue;
+        DeviceProperties dp;
+        dp.device_id = d;
+        dp.compute_capability = p.major * 10 + p.minor;
+        dp.registers_per_block = p.regsPerBlock;
+        dp.registers_per_sm = p.regsPerMultiprocessor;
+        dp.threads_per_block = p.maxThreadsPerBlock;
+        dp.threads_per_sm = p.maxThreadsPerMultiProcessor;
+        dp.warp_size = p.warpSize;
+        dp.memory_bus_width = p.memoryBusWidth;
+        dp.multiprocessor_count = p.multiProcessorCount;
+        dp.total_global_memory = p.totalGlobalMem;
+        dp.shared_memory_per_block = p.sharedMemPerBlock;
+        dp.total_constant_memory = p.totalConstMem;
+        size_t fr = 0, tot = 0;
+        int cur = 0;
+        if (cudaGetDevice(&cur) == cudaSuccess && cudaSetDevice(d) == cudaSuccess) {
+            if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) dp.available_memory = fr;
+            cudaSetDevice(cur);
+        }
+        std::snprintf(dp.device_name, sizeof dp.device_name, "%s", p.name);
+        node.devices.push_back(dp);
+    }
+    node.host.device_count = (int)node.devices.size();
+    c.node_count = 1;
+    c.device_count = node.host.device_count;
+    c.nodes.push_back(node);
+    return c;
+}
+
 namespace Dataset {
+int parse_dataset(const ClusterProperties& cluster_properties, const ProcessingConfig& config,
+                  LocalPartitions& my_partitions) {
+    if (cluster_properties.node_count > 1 || cluster_properties.nodes.size() > 1 || config.total_nodes > 1) {
+        std::cerr << "[" << config.host_name << "] Error: this build trains on one node; "
+                  << std::max<size_t>((size_t)config.total_nodes, cluster_properties.nodes.size())
+                  << " nodes were given." << std::endl;
+        return 1;
+    }
+    LocalPartitions parts;
+    if (parse_dataset(config, parts)) return 1;
+    if (my_partitions.empty()) my_partitions.resize(1);
+    for (Partition& p : my_partitions) p = Partition();
+    my_partitions[0] = std::move(parts[0]);
+    return 0;
+}
+
 int parse_dataset(const ProcessingConfig& config, LocalPartitions& partitions) {
     mc_dataset* d = nullptr;
     if (mc_dataset_parse(config.dataset_path.c_str(), config.max_sessions, config.test_share, &d) != MC_OK) return 1;
@@ -111,6 +193,73 @@ size_t ClickModel_Hst::get_memory_usage() {
     int64_t b = 0;
     if (m_) check(mc_model_memory(m_, &b));
     return (size_t)b;
+}
+
+size_t ClickModel_Hst::compute_memory_footprint(int, int n_qd) {
+    // Rounded as the device arrays are: qd arrays padded to a multiple of 4
+    // plus 4 slots.
+    const size_t qd = (size_t)(((std::max(n_qd, 1) + 3) & ~3) + 4);
+    const size_t n_private = model_type_ == MC_DBN ? 2 : 1;
+    const size_t n_pub = model_type_ == MC_PBM ? 10 : model_type_ == MC_UBM ? 55 : model_type_ == MC_DBN ? 1 : 3;
+    // FP32 values per private parameter; uint2 occurrence / clicked counts and
+    // their packed 16-bit copy; FP32 public values (two halves of 128); FP64
+    // public bins and constants (numerator, denominator).
+    return qd * (4 * n_private + 8 + 4) + 2 * 128 * 4 + 2 * (2 * n_pub * 8);
+}
+
+void ClickModel_Hst::free_device_references() {
+    for (void* a : dev_ref_arrays_) cudaFree(a);
+    dev_ref_arrays_.clear();
+    if (dev_refs_) cudaFree(dev_refs_);
+    if (dev_sizes_) cudaFree(dev_sizes_);
+    dev_refs_ = dev_sizes_ = nullptr;
+}
+
+void ClickModel_Hst::get_device_references(Param**& param_refs, int*& param_sizes) {
+    static_assert(sizeof(Param) == 2 * sizeof(float), "Param must be two floats");
+    if (!m_) throw std::runtime_error("mclicks: get_device_references before init_parameters");
+    free_device_references();
+    int cur = 0;
+    check(cudaGetDevice(&cur) == cudaSuccess ? MC_OK : MC_ERR_CUDA);
+    if (cur != device_ && cudaSetDevice(device_) != cudaSuccess) check(MC_ERR_CUDA);
+    const int n = mc_model_param_count(m_);
+    std::vector<Param*> refs((size_t)n, nullptr);
+    std::vector<int> sizes((size_t)n, 0);
+    auto fail = [&](const char* what) {
+        free_device_references();
+        cudaSetDevice(cur);
+        throw std::runtime_error(std::string("mclicks: get_device_references: ") + what);
+    };
+    for (int i = 0; i < n; i++) {
+        char name[64];
+        int64_t size = 0;
+        int pub = 0;
+        check(mc_model_param_info(m_, i, name, sizeof name, &size, &pub));
+        std::vector<float> v((size_t)size);
+        check(mc_model_get_param(m_, i, v.data(), nullptr));
+        std::vector<Param> host((size_t)size);
+        for (int64_t j = 0; j < size; j++) host[(size_t)j] = Param(v[(size_t)j], 1.f);
+        void* d = nullptr;
+        if (cudaMalloc(&d, std::max<size_t>(1, host.size()) * sizeof(Param)) != cudaSuccess) fail("cudaMalloc failed");
+        dev_ref_arrays_.push_back(d);
+        if (!host.empty() && cudaMemcpy(d, host.data(), host.size() * sizeof(Param), cudaMemcpyHostToDevice) != cudaSuccess)
+            fail("cudaMemcpy failed");
+        refs[(size_t)i] = (Param*)d;
+        sizes[(size_t)i] = (int)size;
+    }
+    if (cudaMalloc(&dev_refs_, std::max(1, n) * sizeof(Param*)) != cudaSuccess ||
+        cudaMalloc(&dev_sizes_, std::max(1, n) * sizeof(int)) != cudaSuccess)
+        fail("cudaMalloc failed");
+    if (cudaMemcpy(dev_refs_, refs.data(), (size_t)n * sizeof(Param*), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dev_sizes_, sizes.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+        fail("cudaMemcpy failed");
+    cudaSetDevice(cur);
+    param_refs = (Param**)dev_refs_;
+    param_sizes = (int*)dev_sizes_;
+}
+
+float ClickModel_Hst::private_value(size_t k, int p) const {
+    return p != -1 ? private_[k][(size_t)p].value() : 1.f / 2.f;
 }
 
 void ClickModel_Hst::get_parameter_information(
@@ -203,14 +352,154 @@ void ClickModel_Hst::set_parameters(std::vector<std::vector<Param>>& source, int
 }
 
 void ClickModel_Hst::destroy_parameters() {
+    free_device_references();
     if (m_) mc_model_destroy(m_);
     m_ = nullptr;
+}
+
+void ClickModel_Hst::set_device(int device, int mode) {
+    if (m_ && (device != device_ || mode != mode_))
+        throw std::runtime_error("mclicks: set_device after init_parameters");
+    device_ = device;
+    mode_ = mode;
 }
 
 void ClickModel_Hst::em(int iterations, int impl) { check(mc_model_em(m_, iterations, impl, nullptr)); }
 
 void ClickModel_Hst::evaluate_device(int which, double& ll_sum, std::array<double, MAX_SERP>& log2_sums, int64_t& n) {
     check(mc_model_evaluate(m_, which, &ll_sum, log2_sums.data(), &n, nullptr));
+}
+
+// ---------------------------------------------------------------------------
+// Per-session probabilities from the host-side values, in FP32 with the
+// reference's expressions (pbm.cu:351-420, ubm.cu:345-468, dbn.cu:572-683,
+// ccm.cu:566-650).
+// ---------------------------------------------------------------------------
+void PBM_Hst::get_serp_probability(SERP_Hst& q, float (&prob)[MAX_SERP]) {
+    for (int r = 0; r < MAX_SERP; r++) prob[r] = private_value(0, q[r].get_param_index()) * public_value((size_t)r);
+}
+
+void PBM_Hst::get_log_conditional_click_probs(SERP_Hst& q, std::vector<float>& out) {
+    for (int r = 0; r < MAX_SERP; r++) {
+        const float ae = private_value(0, q[r].get_param_index()) * public_value((size_t)r);
+        out.push_back(q[r].get_click() == 1 ? std::log(ae) : std::log(1 - ae));
+    }
+}
+
+void PBM_Hst::get_full_click_probs(SERP_Hst& q, std::vector<float>& out) {
+    for (int r = 0; r < MAX_SERP; r++) {
+        const float ae = private_value(0, q[r].get_param_index()) * public_value((size_t)r);
+        out.push_back(q[r].get_click() == 1 ? ae : 1 - ae);
+    }
+}
+
+// UBM examination slot of rank r after a previous click at rank p (9 = none).
+static inline size_t ubm_slot(int r, int p) { return (size_t)(r * (r + 1) / 2 + p); }
+
+void UBM_Hst::get_serp_probability(SERP_Hst& q, float (&prob)[MAX_SERP]) {
+    int prev[MAX_SERP];
+    q.prev_clicked_rank(prev);
+    for (int r = 0; r < MAX_SERP; r++)
+        prob[r] = private_value(0, q[r].get_param_index()) * public_value(ubm_slot(r, prev[r]));
+}
+
+void UBM_Hst::get_log_conditional_click_probs(SERP_Hst& q, std::vector<float>& out) {
+    int prev[MAX_SERP];
+    q.prev_clicked_rank(prev);
+    for (int r = 0; r < MAX_SERP; r++) {
+        const float ae = private_value(0, q[r].get_param_index()) * public_value(ubm_slot(r, prev[r]));
+        out.push_back(q[r].get_click() == 1 ? std::log(ae) : std::log(1 - ae));
+    }
+}
+
+void UBM_Hst::get_full_click_probs(SERP_Hst& q, std::vector<float>& out) {
+    // Marginal click probability of rank r: a sum over the rank of the
+    // previous click (none = -1, whose slot is 9), each term the probability
+    // of that click, of no click in between, and of a click at r.
+    float marg[MAX_SERP];
+    for (int r = 0; r < MAX_SERP; r++) {
+        const float a = private_value(0, q[r].get_param_index());
+        float cp = 0;
+        for (int pc = -1; pc < r; pc++) {
+            const int slot_prev = pc == -1 ? 9 : pc;
+            float none_between = 1.f;
+            for (int b = pc + 1; b < r; b++)
+                none_between *= 1 - private_value(0, q[b].get_param_index()) * public_value(ubm_slot(b, slot_prev));
+            const float t = none_between * (a * public_value(ubm_slot(r, slot_prev)));
+            cp += pc >= 0 ? marg[pc] * t : t;
+        }
+        marg[r] = cp;
+        out.push_back(q[r].get_click() == 1 ? cp : 1 - cp);
+    }
+}
+
+// DBN / CCM: the conditional probability of what happened at each rank,
+// given the ranks before it (get_serp_probability), is also the one whose
+// log the log-likelihood takes.
+void DBN_Hst::get_serp_probability(SERP_Hst& q, float (&prob)[MAX_SERP]) {
+    const float g = public_value(0);
+    float ex = 1.f;
+    for (int r = 0; r < MAX_SERP; r++) {
+        const int p = q[r].get_param_index();
+        const float a = private_value(0, p), sv = private_value(1, p);
+        if (q[r].get_click() == 1) {
+            prob[r] = a * ex;
+            ex = g * (1 - sv);
+        } else {
+            prob[r] = 1 - a * ex;
+            ex *= g * (1 - a) / prob[r];
+        }
+    }
+}
+
+void DBN_Hst::get_log_conditional_click_probs(SERP_Hst& q, std::vector<float>& out) {
+    float cp[MAX_SERP];
+    get_serp_probability(q, cp);
+    for (int r = 0; r < MAX_SERP; r++) out.push_back(std::log(cp[r]));
+}
+
+void DBN_Hst::get_full_click_probs(SERP_Hst& q, std::vector<float>& out) {
+    const float g = public_value(0);
+    float ex = 1.f;
+    for (int r = 0; r < MAX_SERP; r++) {
+        const int p = q[r].get_param_index();
+        const float a = private_value(0, p), sv = private_value(1, p);
+        const float ae = a * ex;
+        out.push_back(q[r].get_click() == 1 ? ae : 1 - ae);
+        ex *= g * (1 - a) + g * a * (1 - sv);
+    }
+}
+
+void CCM_Hst::get_serp_probability(SERP_Hst& q, float (&prob)[MAX_SERP]) {
+    const float t1 = public_value(0), t2 = public_value(1), t3 = public_value(2);
+    float ex = 1.f;
+    for (int r = 0; r < MAX_SERP; r++) {
+        const float a = private_value(0, q[r].get_param_index());
+        if (q[r].get_click() == 1) {
+            prob[r] = a * ex;
+            ex = t2 * (1 - a) + t3 * a;
+        } else {
+            prob[r] = 1 - a * ex;
+            ex *= t1 * (1 - a) / prob[r];
+        }
+    }
+}
+
+void CCM_Hst::get_log_conditional_click_probs(SERP_Hst& q, std::vector<float>& out) {
+    float cp[MAX_SERP];
+    get_serp_probability(q, cp);
+    for (int r = 0; r < MAX_SERP; r++) out.push_back(std::log(cp[r]));
+}
+
+void CCM_Hst::get_full_click_probs(SERP_Hst& q, std::vector<float>& out) {
+    const float t1 = public_value(0), t2 = public_value(1), t3 = public_value(2);
+    float ex = 1.f;
+    for (int r = 0; r < MAX_SERP; r++) {
+        const float a = private_value(0, q[r].get_param_index());
+        const float ae = a * ex;
+        out.push_back(q[r].get_click() == 1 ? ae : 1 - ae);
+        ex *= (1 - a) * t1 + a * ((1 - a) * t2 + a * t3);
+    }
 }
 
 void PBM_Hst::say_hello() { std::cout << "Host-side PBM says hello!" << std::endl; }
@@ -231,22 +520,28 @@ ClickModel_Hst* create_cm_host(int model_type) {
 // Evaluation
 // ---------------------------------------------------------------------------
 float LogLikelihood::evaluate(TestSet& testing_queries) {
-    cm_->upload_test(testing_queries);
-    double ll = 0;
-    std::array<double, MAX_SERP> l2{};
-    int64_t n = 0;
-    cm_->evaluate_device(1, ll, l2, n);
-    return (float)ll;
+    for (SERP_Hst session : testing_queries) {
+        std::vector<float> lp;
+        lp.reserve(MAX_SERP);
+        cm_->get_log_conditional_click_probs(session, lp);
+        llh_values_.push_back(std::accumulate(lp.begin(), lp.end(), 0.f) / MAX_SERP);
+    }
+    return std::accumulate(llh_values_.begin(), llh_values_.end(), 0.f);
 }
 
-void Perplexity::evaluate(ClickModel_Hst* cm, TestSet& testing_queries) {
-    cm->upload_test(testing_queries);
-    double ll = 0;
-    std::array<double, MAX_SERP> l2{};
-    int64_t n = 0;
-    cm->evaluate_device(1, ll, l2, n);
-    task_size = (float)n;
-    for (int r = 0; r < MAX_SERP; r++) task_rank_perplexities[(size_t)r] = (float)l2[(size_t)r];
+void Perplexity::evaluate(ClickModel_Hst* cm, TrainSet& testing_queries) {
+    task_size = static_cast<float>(testing_queries.size());
+    for (SERP_Hst session : testing_queries) {
+        std::vector<float> fp;
+        fp.reserve(MAX_SERP);
+        cm->get_full_click_probs(session, fp);
+        for (int r = 0; r < MAX_SERP; r++) task_rank_perplexities[(size_t)r] += std::log2(fp[(size_t)r]);
+    }
+}
+
+void Perplexity::import(std::array<float, MAX_SERP>& rank_perplexities, float& size) {
+    task_rank_perplexities = rank_perplexities;
+    task_size = size;
 }
 
 // ---------------------------------------------------------------------------
@@ -319,6 +614,7 @@ void em_parallel(const ProcessingConfig& config, LocalPartitions& device_partiti
     using clock = std::chrono::steady_clock;
     std::cout << "\nExpectation Maximization (EM) in parallel ..." << std::endl;
     ClickModel_Hst* cm = create_cm_host(config.model_type);
+    cm->set_device(config.device, config.mode);
     cm->say_hello();
     Partition& part = device_partitions.at(0);
 
