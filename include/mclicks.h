@@ -222,6 +222,16 @@ int mc_model_em_trace(mc_model* m, int32_t n_iterations, double* train_ll, void*
  * model (pbm.cu:191-253, ubm.cu:185-247); this reports which equivalent runs. */
 int mc_model_fused_path(const mc_model* m, int32_t* path, int64_t* n_entries);
 
+/* Testing hook for the timeout path of the fused kernel (the reference stops
+ * the job on an error, communicator.cpp:119-133; here every wait inside a
+ * kernel is bounded and an expired wait surfaces as MC_ERR_DEVICE).  On
+ * `device`, sets the limit of one mbarrier wait to wait_limit_ns (0 restores
+ * the default of 4 s) and makes the stage fill of tile index stall_tile
+ * declare 16 bytes more than it copies, so that the wait for that stage runs
+ * out while every copy has landed (-1: no tile).  Affects every model on the
+ * device until reset; calls that read results then return MC_ERR_DEVICE. */
+int mc_test_wait_hooks(int device, int64_t wait_limit_ns, int32_t stall_tile);
+
 /* Device memory held by the model, in bytes. */
 int mc_model_memory(const mc_model* m, int64_t* bytes);
 
@@ -291,19 +301,27 @@ int mc_dbn_loglik_backward(mc_model* m, int64_t s_begin, int64_t s_count, const 
  * must not enter the allocator (and its implicit synchronisation) while other
  * streams run.  Computes the same sums as mc_model_evaluate from the caller's
  * own device buffers into the caller's host memory, keeping its intermediate
- * sums in a fixed file-scope device array (704 KB on every GPU that loads the
- * library, held until the process exits) instead of an allocation; it calls
- * no allocating CUDA or library routine.
+ * sums in a fixed file-scope device array (768 KB on every GPU where the
+ * library's device code is loaded, held until the process exits) instead of an
+ * allocation; it calls no allocating CUDA or library routine.
  *
+ * model_type: MC_PBM (0), MC_CCM (1), MC_DBN (2) or MC_UBM (3).
  * Limit: n_sessions <= 16,777,216; a larger call fails with MC_ERR_INVALID.
- * Inputs (device memory): pidx session-major [n * 10] (-1 = doc unseen in
- * training), click_mask [n], atr [n_qd], sat [n_qd] (DBN; NULL otherwise),
- * pub = the model's public values (PBM 10, UBM 55, DBN 1, CCM 3).
+ * Inputs (device memory): pidx session-major [n * 10], each -1 (doc unseen in
+ * training) or in [0, n_qd), any other value failing the call with
+ * MC_ERR_INVALID; click_mask [n]; atr [n_qd]; sat [n_qd] (MC_DBN; NULL
+ * otherwise); pub = the model's public values, by model code: MC_PBM 10
+ * examination, MC_CCM 3 continuation, MC_DBN 1 continuation, MC_UBM 55
+ * examination.
  * Outputs (host memory): *ll_sum and log2_sums[10], as mc_model_evaluate.
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture on that device.  All calls share the
- * array: calls that overlap on the GPU race, so serialise them.  Synchronous
- * on `stream`. */
+ * Set-up: the first call on a device makes it current, loads the library's
+ * device code there if CUDA has not yet (which reserves the array) and looks
+ * up the array's device address; a call with n_sessions = 0 does only that.
+ * Make that first call before any stream capture on the device, and before a
+ * pool of the caller's takes the device's free memory.  The address is kept
+ * per device context, and looked up again after cudaDeviceReset.
+ * All calls share the array: calls that overlap on the GPU race, so serialise
+ * them.  Synchronous on `stream`. */
 int mc_evaluate_static(int model_type, int64_t n_sessions, const int32_t* pidx, const uint16_t* click_mask,
                        int64_t n_qd, const float* atr, const float* sat, const float* pub, double* ll_sum,
                        double* log2_sums, void* stream);

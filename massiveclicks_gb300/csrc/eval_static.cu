@@ -10,12 +10,17 @@
 // its intermediate sums in a fixed file-scope device array instead of an
 // allocation.
 //
-// Scratch: g_eval_scratch holds one partial row of 11 doubles per block
-// (log-likelihood sum, then one log2 sum per rank) plus one final row.  Each
-// block covers EVAL_STATIC_SESSIONS_PER_BLOCK sessions, so a call needs
-// ceil(n / 2048) rows; with EVAL_STATIC_MAX_BLOCKS rows the array is 704 KB
-// and the largest accepted n is 16,777,216 sessions.  Every GPU that loads the
-// library holds this array until the process exits.
+// Scratch: g_eval_scratch holds one partial row of 12 doubles per block
+// (log-likelihood sum, one log2 sum per rank, the count of out-of-range
+// indices) plus one final row.  Each block covers
+// EVAL_STATIC_SESSIONS_PER_BLOCK sessions, so a call needs ceil(n / 2048)
+// rows; with EVAL_STATIC_MAX_BLOCKS rows the array is 768 KB and the largest
+// accepted n is 16,777,216 sessions.  Every GPU on which this library's
+// device code is loaded holds the array until the process exits.  CUDA loads
+// device code lazily by default, so the array is reserved on a device by the
+// first call of this entry point there (a call with n_sessions = 0 does only
+// that set-up): a caller whose own pool takes the device memory makes that
+// call first.
 //
 // Every call shares the array and it keeps the last call's contents; a call
 // writes every row it reads before reading it, so nothing needs clearing, but
@@ -27,6 +32,7 @@
 #include <mutex>
 #include <string>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "mclicks.h"
@@ -39,7 +45,8 @@ constexpr int EVAL_STATIC_THREADS = 256;
 constexpr int EVAL_STATIC_SESSIONS_PER_THREAD = 8;
 constexpr int EVAL_STATIC_SESSIONS_PER_BLOCK = EVAL_STATIC_THREADS * EVAL_STATIC_SESSIONS_PER_THREAD;  // 2048
 constexpr int EVAL_STATIC_MAX_BLOCKS = 8192;
-constexpr int EVAL_ROW = MC_R + 1;
+constexpr int EVAL_ROW = MC_R + 2;  // ll, log2 per rank, out-of-range indices
+constexpr int EVAL_SUMS = MC_R + 1;
 constexpr int64_t EVAL_STATIC_MAX_SESSIONS = (int64_t)EVAL_STATIC_SESSIONS_PER_BLOCK * EVAL_STATIC_MAX_BLOCKS;
 
 // Partial rows [0, EVAL_STATIC_MAX_BLOCKS) and the final row after them.
@@ -135,6 +142,7 @@ __global__ void __launch_bounds__(EVAL_STATIC_THREADS) eval_static_kernel(
         for (int r = 0; r < MC_R; r++) {
             int p = pidx[s * MC_R + r];
             bool seen = p >= 0 && (int64_t)p < n_qd;
+            if (!seen && p != -1) acc[EVAL_SUMS] += 1.0;  // neither a pair index nor the unseen marker
             a[r] = seen ? atr[p] : 0.5f;
             sv[r] = (model == MC_DBN && seen) ? sat[p] : 0.5f;
         }
@@ -173,24 +181,67 @@ __global__ void eval_static_reduce_kernel(int blocks, double* scratch) {
     }
 }
 
-// Device address of g_eval_scratch per device, looked up once per device
-// (cudaGetSymbolAddress with that device current) and cached.
+// Device address of g_eval_scratch, looked up with cudaGetSymbolAddress once
+// per device context (with that device current) and cached beside the
+// context's unique id: after cudaDeviceReset the device gets a new primary
+// context with another id, and the address is looked up again.
 constexpr int MAX_DEVICES = 64;
 std::mutex g_addr_mutex;
-double* g_addr[MAX_DEVICES] = {nullptr};
+struct ScratchAddr {
+    double* ptr = nullptr;
+    unsigned long long ctx_id = 0;
+};
+ScratchAddr g_addr[MAX_DEVICES];
 
-int scratch_address(int device, double** out) {
-    std::lock_guard<std::mutex> lock(g_addr_mutex);
-    if (!g_addr[device]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_eval_scratch);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            return mch::set_error(MC_ERR_CUDA, std::string("evaluate_static: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        }
-        g_addr[device] = static_cast<double*>(p);
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+int cuda_fail(const char* what, cudaError_t e) {
+    cudaGetLastError();
+    return mch::set_error(MC_ERR_CUDA, std::string("evaluate_static: ") + what + ": " + cudaGetErrorString(e));
+}
+
+// Id of the context current on this thread (the device's primary context
+// once cudaSetDevice has made it current).
+int current_context_id(unsigned long long* id) {
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+        if (e == cudaSuccess) e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+        if (e != cudaSuccess) return cuda_fail("driver entry points", e);
+        if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return mch::set_error(MC_ERR_CUDA, "evaluate_static: cuCtxGetCurrent / cuCtxGetId unavailable");
+        g_ctx_get_current = (CtxGetCurrentFn)f1;
+        g_ctx_get_id = (CtxGetIdFn)f2;
     }
-    *out = g_addr[device];
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx || g_ctx_get_id(ctx, id) != CUDA_SUCCESS)
+        return mch::set_error(MC_ERR_CUDA, "evaluate_static: no current CUDA context");
+    return MC_OK;
+}
+
+// Makes `device` current (initialising its primary context) and returns the
+// array's address in that context.
+int scratch_address(int device, double** out) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_fail("cudaSetDevice", e);
+    std::lock_guard<std::mutex> lock(g_addr_mutex);
+    unsigned long long id = 0;
+    int rc = current_context_id(&id);
+    if (rc) return rc;
+    ScratchAddr& a = g_addr[device];
+    if (!a.ptr || a.ctx_id != id) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_eval_scratch);
+        if (e != cudaSuccess) return cuda_fail("cudaGetSymbolAddress", e);
+        a.ptr = static_cast<double*>(p);
+        a.ctx_id = id;
+    }
+    *out = a.ptr;
     return MC_OK;
 }
 
@@ -200,7 +251,8 @@ extern "C" int mc_evaluate_static(int model_type, int64_t n_sessions, const int3
                                   int64_t n_qd, const float* atr, const float* sat, const float* pub, double* ll_sum,
                                   double* log2_sums, void* stream) {
     using mch::set_error;
-    if (model_type < 0 || model_type > 3) return set_error(MC_ERR_INVALID, "evaluate_static: model type must be 0..3");
+    if (model_type < 0 || model_type > 3)
+        return set_error(MC_ERR_INVALID, "evaluate_static: model type must be MC_PBM, MC_CCM, MC_DBN or MC_UBM");
     if (n_sessions < 0 || n_qd < 0) return set_error(MC_ERR_INVALID, "evaluate_static: negative size");
     if (n_sessions > EVAL_STATIC_MAX_SESSIONS)
         return set_error(MC_ERR_INVALID, "evaluate_static: " + std::to_string(n_sessions) + " sessions exceed the maximum of " +
@@ -209,18 +261,18 @@ extern "C" int mc_evaluate_static(int model_type, int64_t n_sessions, const int3
     if (!ll_sum || !log2_sums) return set_error(MC_ERR_INVALID, "evaluate_static: null output");
     if (n_sessions > 0 && (!pidx || !click_mask || !atr || !pub || (model_type == MC_DBN && !sat)))
         return set_error(MC_ERR_INVALID, "evaluate_static: null input");
-    if (n_sessions == 0) {
-        *ll_sum = 0.0;
-        for (int r = 0; r < MC_R; r++) log2_sums[r] = 0.0;
-        return MC_OK;
-    }
     int device = 0;
     cudaError_t e = cudaGetDevice(&device);
-    if (e != cudaSuccess) { cudaGetLastError(); return set_error(MC_ERR_CUDA, std::string("evaluate_static: ") + cudaGetErrorString(e)); }
+    if (e != cudaSuccess) return cuda_fail("cudaGetDevice", e);
     if (device < 0 || device >= MAX_DEVICES) return set_error(MC_ERR_INVALID, "evaluate_static: device ordinal too large");
     double* scratch = nullptr;
     int rc = scratch_address(device, &scratch);
     if (rc) return rc;
+    if (n_sessions == 0) {  // the set-up alone
+        *ll_sum = 0.0;
+        for (int r = 0; r < MC_R; r++) log2_sums[r] = 0.0;
+        return MC_OK;
+    }
     cudaStream_t st = (cudaStream_t)stream;
     int blocks = (int)((n_sessions + EVAL_STATIC_SESSIONS_PER_BLOCK - 1) / EVAL_STATIC_SESSIONS_PER_BLOCK);
     eval_static_kernel<<<blocks, EVAL_STATIC_THREADS, 0, st>>>(model_type, n_sessions, n_qd, pidx, click_mask, atr,
@@ -231,7 +283,10 @@ extern "C" int mc_evaluate_static(int model_type, int64_t n_sessions, const int3
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(out, scratch + (int64_t)EVAL_STATIC_MAX_BLOCKS * EVAL_ROW, sizeof(out), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) { cudaGetLastError(); return set_error(MC_ERR_CUDA, std::string("evaluate_static: ") + cudaGetErrorString(e)); }
+    if (e != cudaSuccess) return cuda_fail("evaluation", e);
+    if (out[EVAL_SUMS] != 0.0)
+        return set_error(MC_ERR_INVALID, "evaluate_static: " + std::to_string((int64_t)out[EVAL_SUMS]) +
+                                             " indices are neither -1 nor in [0, n_qd)");
     *ll_sum = out[0];
     for (int r = 0; r < MC_R; r++) log2_sums[r] = out[1 + r];
     return MC_OK;
