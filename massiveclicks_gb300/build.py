@@ -123,9 +123,17 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_LIB
 
 
-def build_reference(ref: str = "/root/reference") -> Path | None:
+# Where build() looks for the reference's sources when MC_REFERENCE_DIR is not
+# set: the read-only checkout of the development container.  Absent elsewhere
+# (the GPU machine, a user's machine), in which case nothing is built.
+REFERENCE_CHECKOUT = "/root/reference"
+
+
+def build_reference(ref: str | None = None) -> Path | None:
     """Compiles the reference's CPU path into oracle/_ref/ when its sources are
-    present (this container only); returns the driver path or None."""
+    present: `ref`, else $MC_REFERENCE_DIR, else REFERENCE_CHECKOUT.  Returns
+    the driver path, or None when no checkout is found."""
+    ref = ref or os.environ.get("MC_REFERENCE_DIR") or REFERENCE_CHECKOUT
     if not Path(ref, "main.cpp").exists():
         return None
     _run(["make", "-s", "-C", str(ORACLE / "ref"), f"REF={ref}", f"-j{os.cpu_count() or 4}"])

@@ -1,8 +1,9 @@
 """Generates the golden vectors under tests/golden/ from the reference itself.
 
-Run in a container that holds the reference sources (default /root/reference):
+Run in a container that holds the reference sources, naming their checkout
+with --ref or the environment variable MC_REFERENCE_DIR:
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref PATH_TO_REFERENCE
 
 For every case it writes a seeded synthetic click log (the package's
 generator, reference text format), compiles the reference's CPU path out of
@@ -21,6 +22,7 @@ ingest (tests/test_ingest.py).  Nothing reads the reference at test time.
 from __future__ import annotations
 
 import argparse
+import os
 import subprocess
 import sys
 import tempfile
@@ -149,8 +151,11 @@ def run_case(driver: Path, name: str, log_text: str, max_sessions: int, models, 
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("MC_REFERENCE_DIR"),
+                    help="checkout of the reference's sources (default: $MC_REFERENCE_DIR)")
     args = ap.parse_args()
+    if not args.ref:
+        sys.exit("name the reference's source checkout with --ref or MC_REFERENCE_DIR")
     build.build_library()
     driver = build.build_reference(args.ref)
     if driver is None:
