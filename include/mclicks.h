@@ -292,6 +292,16 @@ int mc_dbn_loglik_backward(mc_model* m, int64_t s_begin, int64_t s_count, const 
                            const float* gamma, int fp64, double grad_output, float* d_alpha, float* d_beta,
                            float* d_gamma, double* loglik, void* stream);
 
+/* The log-likelihood and its gradient in one pass, without a host round trip
+ * (for a trainer that steps on the device): *d_loglik (a device double)
+ * receives the log-likelihood, d_alpha, d_beta ([n_qd]) and d_gamma ([1])
+ * (device arrays, overwritten) its gradient.  Asynchronous on `stream`.  No
+ * counterpart in the reference (its EM has no gradient); the pair above
+ * computes the same quantities in two calls. */
+int mc_dbn_loglik_grad(mc_model* m, int64_t s_begin, int64_t s_count, const float* alpha, const float* beta,
+                       const float* gamma, int fp64, float* d_alpha, float* d_beta, float* d_gamma, double* d_loglik,
+                       void* stream);
+
 /* ---------------------------------------------------------------------------
  * Allocation-free evaluation.  No counterpart in the reference.
  *

@@ -60,6 +60,7 @@ _SIGS = {
     "mc_model_em_trace": (C.c_int, [_VP, C.c_int32, _VP, _VP]),
     "mc_model_fused_path": (C.c_int, [_VP, C.POINTER(C.c_int32), C.POINTER(_I64)]),
     "mc_model_memory": (C.c_int, [_VP, C.POINTER(_I64)]),
+    "mc_test_wait_hooks": (C.c_int, [C.c_int, _I64, _I32]),
     "mc_empty_cache": (C.c_int, [C.c_int, C.POINTER(_I64)]),
     "mc_cache_bytes": (C.c_int, [C.c_int, C.POINTER(_I64)]),
     "mc_model_destroy": (None, [_VP]),
@@ -70,6 +71,7 @@ _SIGS = {
     "mc_dbn_loglik_forward": (C.c_int, [_VP, _I64, _I64, _VP, _VP, _VP, C.c_int, C.POINTER(_F64), _VP]),
     "mc_dbn_loglik_backward": (C.c_int, [_VP, _I64, _I64, _VP, _VP, _VP, C.c_int, _F64, _VP, _VP, _VP,
                                          C.POINTER(_F64), _VP]),
+    "mc_dbn_loglik_grad": (C.c_int, [_VP, _I64, _I64, _VP, _VP, _VP, C.c_int, _VP, _VP, _VP, _VP, _VP]),
     "mc_evaluate_static": (C.c_int, [C.c_int, _I64, _VP, _VP, _I64, _VP, _VP, _VP, C.POINTER(_F64), _VP, _VP]),
 }
 

@@ -76,7 +76,8 @@ struct TileDev {
     int64_t qd_begin;   // window start
     int64_t blk_off;    // byte offset of the tile's packed block in FitDev::tblk
     int s_packed;       // sessions in the packed block (see pack_tiles_kernel)
-    int pad_;
+    int max_occ;        // largest number of packed (session, rank) entries showing one
+                        // window pair; sets the fixed-point scale of the tile's bins
 };
 
 struct SplitDev {

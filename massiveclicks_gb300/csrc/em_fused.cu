@@ -107,14 +107,23 @@ __device__ __forceinline__ uint64_t global_ns() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
-// Bounded wait: gives up after 4 s of wall-clock time (and, should the timer
-// not advance, after 2^24 rounds of at least 256 ns each).
+// Limit of one mbarrier wait, and a tile index whose stage fill declares 16
+// bytes more than it copies (-1: none), so that the wait for that stage runs
+// out with every copy landed: both set by set_wait_hooks for the tests of the
+// timeout path.
+__device__ unsigned long long g_wait_limit_ns = 4000000000ull;
+__device__ int g_stall_tile = -1;
+
+// Bounded wait: gives up after g_wait_limit_ns of wall-clock time (4 s unless
+// a test shortened it; should the timer not advance, after 2^24 rounds of at
+// least 256 ns each).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = global_ns();
+    const uint64_t limit = g_wait_limit_ns;
     for (uint32_t i = 0; i < (1u << 24); i++) {
         if (mbar_try_wait_for(bar, parity, 200000u)) return true;
-        if (global_ns() - t0 > 4000000000ull) break;
+        if (global_ns() - t0 > limit) break;
         __nanosleep(256);
     }
     atomicOr(status, ST_TIMEOUT);
@@ -196,11 +205,49 @@ struct GlobSrc {
 
 // Statistic k of window entry rl at bins[k * stride + rl]: each statistic is
 // a contiguous array, so the lanes' random entries spread over all 32 banks.
+//
+// A tile's bins hold 32-bit unsigned fixed point, v * 2^shift added with
+// integer atomics, when the tile's shift (fx_scale) allows at least
+// FX_MIN_SHIFT fraction bits; otherwise FP32 added with float atomics.
+// Shared-memory float atomics are several times the cost of integer ones
+// here, and at about nine adds per session they were a third of the launch.
+// The fixed-point sum of a bin is exact (integer addition, any order); each
+// added value carries one rounding of at most 2^-(shift+1).
 struct SmemSink {
     float* bins;
     int stride;
-    __device__ __forceinline__ void add(int rl, int k, float v) const { atomicAdd(bins + k * stride + rl, v); }
+    float scale;  // 2^shift for fixed point, 0 for FP32
+    __device__ __forceinline__ void add(int rl, int k, float v) const {
+        if (scale != 0.0f) atomicAdd(reinterpret_cast<unsigned*>(bins) + k * stride + rl, __float2uint_rn(v * scale));
+        else atomicAdd(bins + k * stride + rl, v);
+    }
 };
+
+// Fixed point needs sum <= 2^31 for every bin: a bin takes at most one value
+// per packed (session, rank) showing its pair, so at most max_occ values (the
+// tile's largest packed occurrence count, found when the tile is packed),
+// each below 2^ev (fx_value_exponent).  shift = 31 - ceil(log2 max_occ) - ev.
+constexpr int FX_MIN_SHIFT = 20;
+
+__device__ __forceinline__ float fx_scale(int max_occ, int ev) {
+    if (max_occ <= 0) return 0.0f;
+    const int need = (max_occ > 1 ? 32 - __clz(max_occ - 1) : 0) + ev;
+    const int shift = 31 - need;
+    return shift >= FX_MIN_SHIFT ? __int_as_float((127 + shift) << 23) : 0.0f;
+}
+
+// ev with every private statistic value below 2^ev, with a factor 2 of margin
+// for rounding.  DBN attractiveness a(1 - eps)/(1 - eps car) and satisfaction
+// s/(1 - (1 - s) g car), the CCM unclicked attractiveness term and the PBM /
+// UBM terms are at most 1 (car <= 1, eps <= 1).  The CCM term of a clicked
+// last rank, a / (1 - (t2 (1 - a) + t3 a) car), is at most 1 / (1 - max(t2, t3)).
+__device__ __forceinline__ int fx_value_exponent(int model, const float* pub) {
+    if (model != CCM) return 1;
+    const float tm = fmaxf(pub[1], pub[2]);
+    const float vb = 2.0f * fmaxf(1.0f, __frcp_ru(1.0f - tm));
+    const unsigned c = (unsigned)fminf(ceilf(vb), 2147483648.0f);
+    return 32 - __clz(c - 1);
+}
 struct GlobSink {
     double* bins;
     int ns;
@@ -616,7 +663,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
         const int64_t a1 = (tile.qd_begin + tile.qd_count + 3) & ~(int64_t)3;
         const uint32_t wn = (uint32_t)(a1 - a0);
         const uint32_t sess = 11u * (uint32_t)((tile.s_packed + 7) & ~7) * 2u;
-        mbar_arrive_expect_tx(&full_bar[st], sess + wn * 4 + (f_sat ? wn * 4 : 0));
+        mbar_arrive_expect_tx(&full_bar[st], sess + wn * 4 + (f_sat ? wn * 4 : 0) + (t == g_stall_tile ? 16u : 0u));
         if (sess) bulk_g2s(sb, reinterpret_cast<const unsigned char*>(f.tblk) + tile.blk_off, sess, &full_bar[st]);
         bulk_g2s(sb + L.atr_off, f.atr + a0, wn * 4, &full_bar[st]);
         if (f_sat) bulk_g2s(sb + L.sat_off, f_sat + a0, wn * 4, &full_bar[st]);
@@ -657,6 +704,8 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
         const int lane = tid & 31;
         const int warp = tid >> 5;
         int cur_fit = -1;
+        int cur_ev = 1;        // fx_value_exponent of the current fit
+        float sc_prev = 0.0f;  // bins scale of the previous tile (0: FP32)
         unsigned cur_count = 0;
         int prev_t = -1;
         int fs = 0, pfs = 0;  // s_fit slots of the current fit and of the previous tile's fit
@@ -742,6 +791,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
                 int it = *(volatile int*)fg.iter;
                 for (int q = ctid; q < fg.n_pub; q += nc) pub_th[q] = fg.pub_theta[(it & 1) * MC_MAX_PUB + q];
                 workers_sync(nc);
+                cur_ev = fx_value_exponent(model_of<MODEL>(s_fit[fs]), pub_th);
             }
             if (warp == 0 && !folded) fold_pub((k - 1) & 1, s_fit[pfs]);
             // Click counts of this tile's window for its M-step (next
@@ -762,6 +812,10 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
 
             // ---- the pool: E-step chunks of tile t, then M-step items of prev_t -
             const bool direct = t >= 0 && tile.qd_count > window_max;
+            const float sc = (t >= 0 && !direct) ? fx_scale(tile.max_occ, cur_ev) : 0.0f;
+            // 2^-shift of the previous tile's bins (exact), 0 for FP32 bins.
+            const float inv_prev = sc_prev != 0.0f ? __frcp_rn(sc_prev) : 0.0f;
+            const unsigned* ubins_m = reinterpret_cast<const unsigned*>(bins) + ((k - 1) & 1) * L.bins_buf;
             const int n_sess = t < 0 ? 0 : (direct ? tile.s_count : tile.s_packed);
             const int nE = (n_sess + 31) >> 5;
             const int nM = prev_t < 0 ? 0 : (ptile.split >= 0 ? 1 : (ptile.qd_count + 32 * kMQ - 1) / (32 * kMQ));
@@ -794,9 +848,16 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
                     for (int j = 0; j < kMQ; j++) {
                         const int i = mi * (32 * kMQ) + j * 32 + lane;
                         if (i < ptile.qd_count) {
-                            float v0 = bins_m[i], v1 = 0.0f;
+                            float v0, v1 = 0.0f;
+                            if (inv_prev != 0.0f) {
+                                v0 = __uint2float_rn(ubins_m[i]) * inv_prev;
+                                if (pns > 1) v1 = __uint2float_rn(ubins_m[L.bins_stride + i]) * inv_prev;
+                            } else {
+                                v0 = bins_m[i];
+                                if (pns > 1) v1 = bins_m[L.bins_stride + i];
+                            }
                             bins_m[i] = 0.0f;
-                            if (pns > 1) { v1 = bins_m[L.bins_stride + i]; bins_m[L.bins_stride + i] = 0.0f; }
+                            if (pns > 1) bins_m[L.bins_stride + i] = 0.0f;
                             const int64_t q = ptile.qd_begin + i;
                             mstep_qd_f(pmodel, pf.mode, make_uint2(pc[j] & 0xFFFFu, pc[j] >> 16), v0, v1, pf.atr + q,
                                        pns > 1 ? pf.sat + q : nullptr);
@@ -809,8 +870,9 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
                 if (ptile.qd_count <= window_max) {
                     for (int i = lane; i < ptile.qd_count; i += 32)
                         for (int kk = 0; kk < pns; kk++) {
-                            float v = bins_m[kk * L.bins_stride + i];
-                            if (v != 0.0f) { atomicAdd(gb + (int64_t)i * pns + kk, (double)v); bins_m[kk * L.bins_stride + i] = 0.0f; }
+                            const int j = kk * L.bins_stride + i;
+                            const double v = inv_prev != 0.0f ? (double)ubins_m[j] * (double)inv_prev : (double)bins_m[j];
+                            if (v != 0.0) { atomicAdd(gb + (int64_t)i * pns + kk, v); bins_m[j] = 0.0f; }
                         }
                 }
                 __threadfence();
@@ -848,7 +910,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             gsrc.pidx = f.pidx; gsrc.clk = f.click; gsrc.atr = f.atr; gsrc.sat = f.sat;
             gsrc.stride = f.stride; gsrc.s_begin = tile.s_begin; gsrc.qd_begin = tile.qd_begin;
             gsrc.qd_count = tile.qd_count; gsrc.status = f.status;
-            SmemSink ssink{bins_e, (int)L.bins_stride};
+            SmemSink ssink{bins_e, (int)L.bins_stride, sc};
             GlobSink gsink{direct ? f.split_bins + splits[tile.split].bin_offset : nullptr,
                            t >= 0 ? private_stats(model) : 1};
 
@@ -919,6 +981,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             if (t < 0) break;
             prev_t = t;
             pfs = fs;
+            sc_prev = sc;
             cur_count++;
         }
         if (cur_fit >= 0 && !*(volatile int*)&s_abort) flush_fit(s_fit[fs], cur_count);
@@ -932,6 +995,12 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             ws->ctas_exited = 0;
         }
     }
+}
+
+cudaError_t set_wait_hooks(unsigned long long wait_limit_ns, int stall_tile) {
+    cudaError_t e = cudaMemcpyToSymbol(g_wait_limit_ns, &wait_limit_ns, sizeof wait_limit_ns);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_stall_tile, &stall_tile, sizeof stall_tile);
+    return e;
 }
 
 size_t fused_smem_bytes(int model, int window_max, int spt, int n_stages) {
@@ -1020,14 +1089,16 @@ __device__ __forceinline__ void pack_sort(PackSortStorage& tmp, uint32_t* keys, 
 }
 
 __global__ void __launch_bounds__(kPackThreads) pack_tiles_kernel(int model, TileDev* tiles, int n_tiles, int window_max,
-                                                                 const int32_t* planes, int64_t stride,
+                                                                 int n_keys, const int32_t* planes, int64_t stride,
                                                                  const uint16_t* click, unsigned char* tblk, int* status) {
-    extern __shared__ uint32_t keys[];
+    extern __shared__ uint32_t keys[];   // [n_keys] sort keys, then [window_max] occurrence counts
     __shared__ PackSortStorage sort_tmp;
-    __shared__ int s_kept;
+    __shared__ int s_kept, s_max_occ;
+    unsigned* occ = keys + n_keys;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
         const TileDev tile = tiles[t];
         if (tile.qd_count > window_max) continue;
+        for (int i = threadIdx.x; i < tile.qd_count; i += blockDim.x) occ[i] = 0;
         const bool drop_clickless = model == DBN || model == CCM;
         if (tile.s_count <= 4 * kPackThreads)
             pack_sort<4>(sort_tmp, keys, click, tile.s_begin, tile.s_count, drop_clickless);
@@ -1051,6 +1122,7 @@ __global__ void __launch_bounds__(kPackThreads) pack_tiles_kernel(int model, Til
         const int spad = (n_kept + 7) & ~7;
         uint16_t* rel = reinterpret_cast<uint16_t*>(tblk + tile.blk_off);
         uint16_t* clk = rel + 10 * spad;
+        if (threadIdx.x == 0) s_max_occ = 0;
         for (int i = threadIdx.x; i < spad; i += blockDim.x) {
             bool in = i < n_kept;
             int64_t s = tile.s_begin + (in ? (int64_t)(keys[i] & 0xFFFFu) : 0);
@@ -1058,10 +1130,19 @@ __global__ void __launch_bounds__(kPackThreads) pack_tiles_kernel(int model, Til
                 int64_t p = in ? (int64_t)planes[(int64_t)r * stride + s] - tile.qd_begin : 0;
                 if (p < 0 || p >= tile.qd_count) { atomicOr(status, ST_BAD_INDEX); p = 0; }
                 rel[r * spad + i] = (uint16_t)p;
+                if (in) atomicAdd(occ + p, 1u);
             }
             clk[i] = in ? click[s] : (uint16_t)0;
         }
-        if (threadIdx.x == 0) tiles[t].s_packed = n_kept;
+        __syncthreads();
+        unsigned mx = 0;
+        for (int i = threadIdx.x; i < tile.qd_count; i += blockDim.x) mx = occ[i] > mx ? occ[i] : mx;
+        if (mx) atomicMax(&s_max_occ, (int)mx);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            tiles[t].s_packed = n_kept;
+            tiles[t].max_occ = s_max_occ;
+        }
         __syncthreads();
     }
 }
@@ -1074,8 +1155,13 @@ cudaError_t launch_pack_tiles(int model, TileDev* tiles, int n_tiles, int window
     int P = kPackMinKeys;
     while (P < max_tile_sessions) P <<= 1;
     int g = n_tiles < 8 * n_sm ? n_tiles : 8 * n_sm;
-    pack_tiles_kernel<<<g, kPackThreads, (size_t)P * 4, st>>>(model, tiles, n_tiles, window_max, planes, stride, click,
-                                                              tblk, status);
+    const size_t smem = ((size_t)P + (size_t)window_max) * 4;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(pack_tiles_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    pack_tiles_kernel<<<g, kPackThreads, smem, st>>>(model, tiles, n_tiles, window_max, P, planes, stride, click, tblk,
+                                                     status);
     return cudaGetLastError();
 }
 

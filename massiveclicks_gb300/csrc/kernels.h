@@ -13,6 +13,9 @@ namespace mcd {
 size_t fused_smem_bytes(int model, int window_max, int spt, int n_stages);
 cudaError_t fused_set_smem_limits(size_t bytes);
 cudaError_t fused_occupancy(int model, int block, size_t smem, int* blocks_per_sm);
+// Wait limit of the fused kernel's mbarrier waits and a tile whose stage is
+// made to stall (-1: none), on the current device; for the timeout tests.
+cudaError_t set_wait_hooks(unsigned long long wait_limit_ns, int stall_tile);
 cudaError_t launch_em_fused(int model, const FitDev* fits, const TileDev* tiles, int n_tiles, const SplitDev* splits,
                             WorkState* ws, int window_max, int spt, int n_stages, int grid, int block,
                             cudaStream_t stream);
@@ -102,6 +105,10 @@ struct AdjointArgs {
 };
 
 cudaError_t launch_adjoint(const AdjointArgs& A, bool grad, bool fp64, int n_sm, cudaStream_t st);
+// Tiles [t0, t1) of a model whose sessions are grouped by query; sessions
+// outside [A.begin, A.begin + A.count) are skipped.
+cudaError_t launch_adjoint_tiles(const AdjointArgs& A, const TileDev* tiles, int t0, int t1, int window_max, bool grad,
+                                 bool fp64, int n_sm, cudaStream_t st);
 cudaError_t launch_grad_to_float(const double* src, float* dst, int64_t n, int n_sm, cudaStream_t st);
 
 }  // namespace mcd

@@ -353,6 +353,7 @@ struct mc_model {
     WorkState* d_ws = nullptr;
     int n_tiles = 0, n_splits = 0, grid = 0;
     bool tiles_ready = false;  // tiles built for the current shape (PBM/UBM build them only for batches)
+    std::vector<int64_t> h_tile_begin;  // first session of each tile, ascending (adjoint range lookups)
     unsigned char* d_tblk = nullptr;
     int64_t split_bins_count = 0;
     int64_t tile_bytes = 0;
@@ -412,6 +413,7 @@ struct mc_model {
         bytes -= tile_bytes;
         tile_bytes = 0;
         tiles_ready = false;
+        h_tile_begin.clear();
     }
 
     void free_plain() {
@@ -654,6 +656,9 @@ int mc_model::build_tiles() {
         }
     }
     n_tiles = (int)tiles.size();
+    h_tile_begin.resize(tiles.size());
+    for (size_t i = 0; i < tiles.size(); i++) h_tile_begin[i] = tiles[i].s_begin;
+    if (!std::is_sorted(h_tile_begin.begin(), h_tile_begin.end())) h_tile_begin.clear();  // no range lookups
     n_splits = (int)splits.size();
     split_bins_count = bin_off;
     int64_t before = bytes;
@@ -1225,7 +1230,21 @@ static int check_status(mc_model* m, cudaStream_t st) {
     CK(cudaStreamSynchronize(st));
     int status = 0;
     CK(cudaMemcpy(&status, m->d_status, 4, cudaMemcpyDeviceToHost));
+    if (status & ST_TIMEOUT)
+        return set_error(MC_ERR_DEVICE, "a kernel's wait for a tile's data timed out; the fit's results are incomplete (status " +
+                                            std::to_string(status) + ")");
     if (status) return set_error(MC_ERR_DEVICE, "kernel reported a parameter index outside its query's window (status " + std::to_string(status) + ")");
+    return MC_OK;
+}
+
+extern "C" int mc_test_wait_hooks(int device, int64_t wait_limit_ns, int32_t stall_tile) {
+    if (wait_limit_ns < 0 || stall_tile < -1) return set_error(MC_ERR_INVALID, "test_wait_hooks: bad argument");
+    int cur = 0;
+    CK(cudaGetDevice(&cur));
+    CK(cudaSetDevice(device));
+    cudaError_t e = mcd::set_wait_hooks(wait_limit_ns ? (unsigned long long)wait_limit_ns : 4000000000ull, stall_tile);
+    cudaSetDevice(cur);
+    CK(e);
     return MC_OK;
 }
 
@@ -1690,6 +1709,20 @@ static AdjointArgs adjoint_args(mc_model* m, int64_t s_begin, int64_t s_count, c
     return A;
 }
 
+// Through the tiles when the sessions are grouped by query (tiles built),
+// else one thread per session with global atomics.
+static cudaError_t run_adjoint(mc_model* m, const AdjointArgs& A, bool grad, bool fp64, cudaStream_t st) {
+    if (m->fused_ok && m->tiles_ready && !m->h_tile_begin.empty()) {
+        const auto& tb = m->h_tile_begin;
+        // tiles [t0, t1) intersect [begin, begin + count): tile starts ascend
+        int t0 = (int)(std::upper_bound(tb.begin(), tb.end(), A.begin) - tb.begin()) - 1;
+        if (t0 < 0) t0 = 0;
+        const int t1 = (int)(std::lower_bound(tb.begin(), tb.end(), A.begin + A.count) - tb.begin());
+        return launch_adjoint_tiles(A, m->d_tiles, t0, t1, m->wqd, grad, fp64, m->n_sm, st);
+    }
+    return launch_adjoint(A, grad, fp64, m->n_sm, st);
+}
+
 extern "C" int mc_dbn_loglik_forward(mc_model* m, int64_t s_begin, int64_t s_count, const float* alpha,
                                      const float* beta, const float* gamma, int fp64, double* loglik, void* stream) {
     int rc = adjoint_common(m, s_begin, s_count, alpha, beta, gamma, "dbn_loglik_forward");
@@ -1698,7 +1731,7 @@ extern "C" int mc_dbn_loglik_forward(mc_model* m, int64_t s_begin, int64_t s_cou
     cudaStream_t st = m->pick(stream);
     AdjointArgs A = adjoint_args(m, s_begin, s_count, alpha, beta, gamma, 0.0);
     CK(cudaMemsetAsync(A.ll_out, 0, 8, st));
-    CK(launch_adjoint(A, false, fp64 != 0, m->n_sm, st));
+    CK(run_adjoint(m, A, false, fp64 != 0, st));
     CK(cudaMemcpyAsync(loglik, A.ll_out, 8, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     return MC_OK;
@@ -1713,7 +1746,7 @@ extern "C" int mc_dbn_loglik_backward(mc_model* m, int64_t s_begin, int64_t s_co
     cudaStream_t st = m->pick(stream);
     AdjointArgs A = adjoint_args(m, s_begin, s_count, alpha, beta, gamma, grad_output);
     CK(cudaMemsetAsync(m->d_grad, 0, (size_t)(2 * m->qd_alloc() + 2) * 8, st));
-    CK(launch_adjoint(A, true, fp64 != 0, m->n_sm, st));
+    CK(run_adjoint(m, A, true, fp64 != 0, st));
     CK(launch_grad_to_float(A.g_alpha, d_alpha, m->n_qd, m->n_sm, st));
     CK(launch_grad_to_float(A.g_beta, d_beta, m->n_qd, m->n_sm, st));
     CK(launch_grad_to_float(A.g_gamma, d_gamma, 1, m->n_sm, st));
@@ -1723,5 +1756,23 @@ extern "C" int mc_dbn_loglik_backward(mc_model* m, int64_t s_begin, int64_t s_co
     } else if (!stream) {
         CK(cudaStreamSynchronize(st));
     }
+    return MC_OK;
+}
+
+extern "C" int mc_dbn_loglik_grad(mc_model* m, int64_t s_begin, int64_t s_count, const float* alpha, const float* beta,
+                                  const float* gamma, int fp64, float* d_alpha, float* d_beta, float* d_gamma,
+                                  double* d_loglik, void* stream) {
+    int rc = adjoint_common(m, s_begin, s_count, alpha, beta, gamma, "dbn_loglik_grad");
+    if (rc) return rc;
+    if (!d_alpha || !d_beta || !d_gamma || !d_loglik) return set_error(MC_ERR_INVALID, "dbn_loglik_grad: null output");
+    cudaStream_t st = m->pick(stream);
+    AdjointArgs A = adjoint_args(m, s_begin, s_count, alpha, beta, gamma, 1.0);
+    CK(cudaMemsetAsync(m->d_grad, 0, (size_t)(2 * m->qd_alloc() + 2) * 8, st));
+    CK(run_adjoint(m, A, true, fp64 != 0, st));
+    CK(launch_grad_to_float(A.g_alpha, d_alpha, m->n_qd, m->n_sm, st));
+    CK(launch_grad_to_float(A.g_beta, d_beta, m->n_qd, m->n_sm, st));
+    CK(launch_grad_to_float(A.g_gamma, d_gamma, 1, m->n_sm, st));
+    CK(cudaMemcpyAsync(d_loglik, A.ll_out, 8, cudaMemcpyDeviceToDevice, st));
+    if (!stream) CK(cudaStreamSynchronize(st));
     return MC_OK;
 }

@@ -253,3 +253,45 @@ def test_reference_f32_error_budget():
     cm = gpu_fit(case, 2, 20)
     gpu_err = np.max(np.abs(cm.flat_parameters().astype(np.float64) - f64) / np.abs(f64))
     assert gpu_err <= max(ref_err, PARAM_RTOL)
+
+
+def test_float_bins_when_fixed_point_lacks_bits():
+    """Tiles accumulate in 32-bit fixed point when the tile's largest
+    occurrence count leaves at least 20 fraction bits, else in FP32.  A query
+    with 3,000 sessions over 12 documents in one 4,096-session tile (a
+    document shown about 2,500 times) takes the FP32 bins; both kinds of tile
+    must match the oracle."""
+    rng = np.random.default_rng(5)
+    n = 3000
+    query = np.zeros(n, np.int32)
+    docs = np.stack([rng.permutation(12)[:10] for _ in range(n)]).astype(np.int32)
+    masks = rng.integers(0, 1024, n).astype(np.uint16)
+    ds = api.Dataset.from_sessions(query, docs, masks, 0.0)
+    for model in (2, 1):
+        f = bindings.OracleFit("f64", model, 0, ds.train.query, ds.train.pidx, ds.train.click, ds.n_qd)
+        f.run(5)
+        for config in ((4096, 1024, 256), (256, 1024, 256)):
+            cm = api.ClickModel.create(model)
+            cm.upload(ds.train, ds.n_qd)
+            cm.configure(*config)
+            cm.em(5)
+            assert_params_close(cm.get_parameters(), f.values(), what=f"m{model} {config}")
+
+
+def test_ccm_large_continuation_bounds_the_scale():
+    """The CCM term of a clicked last rank grows as 1 / (1 - max(t2, t3));
+    with t2 near the clamp the fixed-point scale drops and the tiles fall back
+    to FP32 bins.  One iteration from the same parameters as the oracle."""
+    case = load_case("ccm_ccmclicks")
+    rng = np.random.default_rng(9)
+    n_qd = int(case["n_qd"])
+    values = {"attractiveness": rng.uniform(0.05, 0.95, n_qd).astype(np.float32),
+              "continuation": np.array([0.6, 0.999999, 0.2], np.float32)}
+    cm = api.ClickModel.create(1)
+    cm.upload(sset(case, "train"), n_qd)
+    cm.set_parameters(values)
+    cm.em(1)
+    f = bindings.OracleFit("f64", 1, 0, case["train_query"], case["train_pidx"], case["train_click"], n_qd)
+    f.set_values({k: v.astype(np.float64) for k, v in values.items()})
+    f.run(1)
+    assert_params_close(cm.get_parameters(), f.values(), what="ccm t2 near 1")
