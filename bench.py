@@ -624,26 +624,48 @@ def run_adjoint(args, rank: int, world: int, local: int):
     target = max(ll for _, ll in em_curve)  # EM's best test LL within 50 iterations
     t_em_target = next(t for t, ll in em_curve if ll >= target - 1e-4 * abs(target))
 
+    # Adam's minibatches: consecutive ranges of a random order of whole
+    # queries (unbiased, and the adjoint's tile path applies).
+    t_sessions, t_nqd, to_orig = gradient.query_order(ds.train, seed=rank)
+    assert t_nqd == n_qd
     trainer_model = api.DBNModel(device=local)
-    trainer_model.upload(gradient.shuffled_sessions(ds.train, seed=rank), n_qd)
-    evaluator = api.DBNModel(device=local)
-    evaluator.init_parameters(ds)
+    trainer_model.upload(t_sessions, n_qd)
+    # Test-set evaluation from the logits on the device (mc_evaluate_static),
+    # outside the trainer's clock.
+    lib = api._capi.load()
+    dev = torch.device("cuda", local)
+    to_orig_t = torch.from_numpy(to_orig).to(dev)
+    test_pidx = torch.from_numpy(np.ascontiguousarray(ds.test.pidx, np.int32).reshape(-1)).to(dev)
+    test_click = torch.from_numpy(np.ascontiguousarray(ds.test.click, np.uint16).view(np.int16)).to(dev)
+    n_test = len(ds.test)
     curve = []
+    import ctypes as C
+
+    def test_llh(a, b, g):
+        atr = torch.empty(n_qd, dtype=torch.float32, device=dev)
+        sat = torch.empty(n_qd, dtype=torch.float32, device=dev)
+        atr[to_orig_t] = torch.sigmoid(a.detach())
+        sat[to_orig_t] = torch.sigmoid(b.detach())
+        pub = torch.sigmoid(g.detach()).contiguous()
+        torch.cuda.synchronize()
+        ll = C.c_double()
+        l2 = np.zeros(10)
+        api.check(lib.mc_evaluate_static(2, n_test, C.c_void_p(test_pidx.data_ptr()), C.c_void_p(test_click.data_ptr()),
+                                         n_qd, C.c_void_p(atr.data_ptr()), C.c_void_p(sat.data_ptr()),
+                                         C.c_void_p(pub.data_ptr()), C.byref(ll), l2.ctypes.data_as(C.c_void_p), None))
+        return ll.value / n_test
 
     def cb(step, seconds, a, b, g):
-        evaluator.set_parameters(gradient.logits_to_values(a, b, g))
-        curve.append((step, seconds, evaluator.evaluate(1).llh))
+        curve.append((step, seconds, test_llh(a, b, g)))
 
     batch = 262_144
     steps_per_epoch = (n_train + batch - 1) // batch
     gradient.train_adam(trainer_model, n_qd, steps=20 * steps_per_epoch, batch=batch, lr=0.05, callback=cb,
                         callback_every=steps_per_epoch, device=local)
-    # evaluation time is excluded: subtract nothing from seconds (the callback
-    # runs between timed segments), so report the trainer's own clock
     reach = next(((s, t, ll) for s, t, ll in curve if ll >= target - 1e-4 * abs(target)), None)
+    t_steps = curve[-1][1] if curve else None
 
     # adjoint throughput: one forward + backward over all training sessions
-    dev = torch.device("cuda", local)
     a = torch.zeros(n_qd, device=dev, requires_grad=True)
     b = torch.zeros(n_qd, device=dev, requires_grad=True)
     g = torch.zeros(1, device=dev, requires_grad=True)
@@ -671,8 +693,11 @@ def run_adjoint(args, rank: int, world: int, local: int):
             "adam": {"reached": reach is not None, "steps": reach[0] if reach else None,
                      "seconds": reach[1] if reach else None, "final_test_llh": curve[-1][2] if curve else None,
                      "best_test_llh": max(ll for _, _, ll in curve) if curve else None},
+            "adam_ms_per_step": 1000.0 * t_steps / (20 * steps_per_epoch) if t_steps else None,
             "adjoint": {"ms_per_forward_backward": ms_grad,
-                        "session_gradients_per_s": n_train / (ms_grad / 1000.0)},
+                        "session_gradients_per_s": n_train / (ms_grad / 1000.0),
+                        "em_session_iterations_per_s": n_train * 50 / t_em,
+                        "path": "tiles (sessions grouped by query, gradient summed per tile in shared memory)"},
         }
         print(json.dumps(line), flush=True)
 

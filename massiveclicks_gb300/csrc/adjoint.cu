@@ -10,7 +10,9 @@
 // and LL = sum_r log p_r.  One thread per session runs this recursion forward,
 // keeps the ten examination messages in registers, and walks it back
 // (reverse mode) to the adjoints of a, s and g; the messages are recomputed
-// by every call instead of being stored.  Gradients are accumulated in FP64.
+// by every call instead of being stored.  Sessions grouped by query go
+// through the model's tiles, with the gradient summed per tile in shared
+// memory; other session orders through FP64 global atomics per session.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -105,6 +107,127 @@ __global__ void __launch_bounds__(256) adjoint_kernel(AdjointArgs A, bool grad) 
     }
 }
 
+// Tile path (sessions grouped by query, as the model's tiles describe them):
+// a block takes whole tiles; a tile whose query-document window fits in
+// shared memory gets its window's values sigmoid(alpha), sigmoid(beta)
+// staged once and its gradient summed in shared memory, then written out in
+// one pass per window entry: a plain store for a tile that owns its window
+// (whole queries: no other tile touches those pairs), FP64 atomics for a
+// chunk of a split query.  A wider window takes the per-session kernel's
+// global atomics.  The continuation gradient and the log-likelihood go
+// through registers and one FP64 atomic per block.
+template <typename T>
+__global__ void __launch_bounds__(256) adjoint_tiles_kernel(AdjointArgs A, const TileDev* __restrict__ tiles, int t0,
+                                                           int t1, int window_max, bool grad) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    T* va = reinterpret_cast<T*>(sm);             // [window_max] attractiveness of the window
+    T* vs = va + window_max;                       // [window_max] satisfaction
+    T* ga = vs + window_max;                       // [window_max] gradient sums (alpha)
+    T* gb = ga + window_max;                       // [window_max] gradient sums (beta)
+    __shared__ double red[2][8];
+    const T g = sigm<T>(A.gamma[0]);
+    const T w = (T)A.scale;
+    double ll = 0.0;
+    T g_bar_acc = T(0);
+    const int64_t r0 = A.begin, r1 = A.begin + A.count;
+    for (int t = t0 + blockIdx.x; t < t1; t += gridDim.x) {
+        const TileDev tile = tiles[t];
+        const int64_t s0 = tile.s_begin > r0 ? tile.s_begin : r0;
+        const int64_t s1 = tile.s_begin + tile.s_count < r1 ? tile.s_begin + tile.s_count : r1;
+        if (s0 >= s1) continue;  // uniform over the block
+        const bool staged = tile.qd_count <= window_max;
+        if (staged) {
+            for (int i = threadIdx.x; i < tile.qd_count; i += blockDim.x) {
+                va[i] = sigm<T>(A.alpha[tile.qd_begin + i]);
+                vs[i] = sigm<T>(A.beta[tile.qd_begin + i]);
+                ga[i] = T(0);
+                gb[i] = T(0);
+            }
+            __syncthreads();
+        }
+        for (int64_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+            int rl[MC_R];
+            T a[MC_R], sv[MC_R], ex[MC_R + 1], pr[MC_R];
+            const unsigned m = A.click[s];
+#pragma unroll
+            for (int r = 0; r < MC_R; r++) {
+                const int p = A.pidx[(int64_t)r * A.stride + s];
+                // A tile's sessions show only its window's pairs (the tiles
+                // are built so); the clamp keeps shared-memory accesses in
+                // bounds regardless.
+                rl[r] = staged ? min(max(p - (int)tile.qd_begin, 0), tile.qd_count - 1) : p;
+                a[r] = staged ? va[rl[r]] : sigm<T>(A.alpha[p]);
+                sv[r] = staged ? vs[rl[r]] : sigm<T>(A.beta[p]);
+            }
+            ex[0] = T(1);
+            T lls = T(0);
+#pragma unroll
+            for (int r = 0; r < MC_R; r++) {
+                if ((m >> r) & 1u) {
+                    pr[r] = a[r] * ex[r];
+                    ex[r + 1] = g * (T(1) - sv[r]);
+                } else {
+                    pr[r] = T(1) - a[r] * ex[r];
+                    ex[r + 1] = ex[r] * g * (T(1) - a[r]) / pr[r];
+                }
+                lls += tlog(pr[r]);
+            }
+            ll += (double)lls;
+            if (!grad) continue;
+            T e_bar = T(0);
+#pragma unroll
+            for (int r = MC_R - 1; r >= 0; r--) {
+                T a_bar, ex_bar;
+                if ((m >> r) & 1u) {
+                    a_bar = T(1) / a[r];
+                    ex_bar = T(1) / ex[r];
+                    g_bar_acc += e_bar * (T(1) - sv[r]);
+                    const T db = w * (-e_bar * g) * sv[r] * (T(1) - sv[r]);
+                    if (staged) atomicAdd(gb + rl[r], db);
+                    else atomicAdd(A.g_beta + rl[r], (double)db);
+                } else {
+                    const T ip = T(1) / pr[r];
+                    a_bar = -ex[r] * ip + e_bar * ex[r] * g * (ex[r] - T(1)) * ip * ip;
+                    ex_bar = -a[r] * ip + e_bar * g * (T(1) - a[r]) * ip * ip;
+                    g_bar_acc += e_bar * ex[r] * (T(1) - a[r]) * ip;
+                }
+                const T da = w * a_bar * a[r] * (T(1) - a[r]);
+                if (staged) atomicAdd(ga + rl[r], da);
+                else atomicAdd(A.g_alpha + rl[r], (double)da);
+                e_bar = ex_bar;
+            }
+        }
+        if (staged) {
+            __syncthreads();
+            if (grad) {
+                const bool owned = tile.split < 0;
+                for (int i = threadIdx.x; i < tile.qd_count; i += blockDim.x) {
+                    const int64_t q = tile.qd_begin + i;
+                    if (owned) {
+                        A.g_alpha[q] = (double)ga[i];
+                        A.g_beta[q] = (double)gb[i];
+                    } else {
+                        if (ga[i] != T(0)) atomicAdd(A.g_alpha + q, (double)ga[i]);
+                        if (gb[i] != T(0)) atomicAdd(A.g_beta + q, (double)gb[i]);
+                    }
+                }
+            }
+            __syncthreads();  // the window arrays are reused by the next tile
+        }
+    }
+    double gg = grad ? (double)(w * g_bar_acc * g * (T(1) - g)) : 0.0;
+    ll = warp_sum_dd(ll);
+    gg = warp_sum_dd(gg);
+    if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = ll; red[1][threadIdx.x >> 5] = gg; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double v = 0.0, u = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) { v += red[0][k]; u += red[1][k]; }
+        atomicAdd(A.ll_out, v);
+        if (grad && u != 0.0) atomicAdd(A.g_gamma, u);
+    }
+}
+
 __global__ void grad_to_float_kernel(const double* src, float* dst, int64_t n) {
     int64_t step = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) dst[i] = (float)src[i];
@@ -116,6 +239,27 @@ cudaError_t launch_adjoint(const AdjointArgs& A, bool grad, bool fp64, int n_sm,
     int g = (int)(blocks < 8 * n_sm ? blocks : 8 * n_sm);
     if (fp64) adjoint_kernel<double><<<g, 256, 0, st>>>(A, grad);
     else adjoint_kernel<float><<<g, 256, 0, st>>>(A, grad);
+    return cudaGetLastError();
+}
+
+size_t adjoint_tiles_smem(int window_max, bool fp64) { return (size_t)4 * window_max * (fp64 ? 8 : 4); }
+
+cudaError_t launch_adjoint_tiles(const AdjointArgs& A, const TileDev* tiles, int t0, int t1, int window_max, bool grad,
+                                 bool fp64, int n_sm, cudaStream_t st) {
+    if (A.count <= 0 || t1 <= t0) return cudaSuccess;
+    const size_t smem = adjoint_tiles_smem(window_max, fp64);
+    cudaError_t e = fp64 ? cudaFuncSetAttribute(adjoint_tiles_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                         : cudaFuncSetAttribute(adjoint_tiles_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = fp64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_tiles_kernel<double>, 256, smem)
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_tiles_kernel<float>, 256, smem);
+    if (e != cudaSuccess) return e;
+    const int n = t1 - t0;
+    const int cap = (per_sm > 0 ? per_sm : 1) * n_sm;
+    const int g = n < cap ? n : cap;
+    if (fp64) adjoint_tiles_kernel<double><<<g, 256, smem, st>>>(A, tiles, t0, t1, window_max, grad);
+    else adjoint_tiles_kernel<float><<<g, 256, smem, st>>>(A, tiles, t0, t1, window_max, grad);
     return cudaGetLastError();
 }
 

@@ -1,13 +1,18 @@
 """Gradient-based DBN training beside EM.
 
-``DBNLogLikelihood`` is a torch autograd Function over the C-ABI pair
-``mc_dbn_loglik_forward`` / ``mc_dbn_loglik_backward``: the DBN session
-log-likelihood (the reference's conditional click model, dbn.cu:611-639) of a
-range of a model's uploaded training sessions as a function of logit
-parameters alpha (attractiveness), beta (satisfaction), gamma (continuation).
-Its backward pass is the hand-written adjoint kernel.
+``DBNLogLikelihood`` is a torch autograd Function over the C-ABI: the DBN
+session log-likelihood (the reference's conditional click model,
+dbn.cu:611-639) of a range of a model's uploaded training sessions as a
+function of logit parameters alpha (attractiveness), beta (satisfaction),
+gamma (continuation).  When a gradient is wanted, the forward pass runs the
+hand-written adjoint kernel once (``mc_dbn_loglik_grad``: log-likelihood and
+gradient, no host round trip) and the backward pass scales the stored
+gradient; otherwise it runs ``mc_dbn_loglik_forward``.
 
 ``train_adam`` fits the logits with torch's Adam on minibatches of sessions.
+``query_order`` lays sessions out in a random order of whole queries, so that
+consecutive ranges are random sets of queries (unbiased minibatches) while
+each query's sessions stay together (the adjoint's tile path).
 """
 from __future__ import annotations
 
@@ -40,23 +45,27 @@ def _function():
             for t in (alpha, beta, gamma):
                 if t.dtype != torch.float32 or not t.is_cuda or not t.is_contiguous():
                     raise TypeError("alpha, beta and gamma must be contiguous float32 CUDA tensors")
+            lib = _capi.load()
+            if any(ctx.needs_input_grad[:3]):
+                ll = torch.empty((), dtype=torch.float64, device=alpha.device)
+                da = torch.empty_like(alpha)
+                db = torch.empty_like(beta)
+                dg = torch.empty_like(gamma)
+                check(lib.mc_dbn_loglik_grad(model._h, int(begin), int(count), _ptr(alpha), _ptr(beta), _ptr(gamma),
+                                             int(bool(fp64)), _ptr(da), _ptr(db), _ptr(dg), _ptr(ll),
+                                             _stream_handle()))
+                ctx.save_for_backward(da, db, dg)
+                return ll
             ll = C.c_double()
-            check(_capi.load().mc_dbn_loglik_forward(model._h, int(begin), int(count), _ptr(alpha), _ptr(beta),
-                                                     _ptr(gamma), int(bool(fp64)), C.byref(ll), _stream_handle()))
-            ctx.save_for_backward(alpha, beta, gamma)
-            ctx.model, ctx.begin, ctx.count, ctx.fp64 = model, int(begin), int(count), bool(fp64)
+            check(lib.mc_dbn_loglik_forward(model._h, int(begin), int(count), _ptr(alpha), _ptr(beta), _ptr(gamma),
+                                            int(bool(fp64)), C.byref(ll), _stream_handle()))
             return torch.tensor(ll.value, dtype=torch.float64, device=alpha.device)
 
         @staticmethod
         def backward(ctx, grad_out):
-            alpha, beta, gamma = ctx.saved_tensors
-            da = torch.empty_like(alpha)
-            db = torch.empty_like(beta)
-            dg = torch.empty_like(gamma)
-            check(_capi.load().mc_dbn_loglik_backward(ctx.model._h, ctx.begin, ctx.count, _ptr(alpha), _ptr(beta),
-                                                      _ptr(gamma), int(ctx.fp64), float(grad_out), _ptr(da), _ptr(db),
-                                                      _ptr(dg), None, _stream_handle()))
-            return da, db, dg, None, None, None, None
+            da, db, dg = ctx.saved_tensors
+            w = grad_out.to(torch.float32)
+            return da * w, db * w, dg * w, None, None, None, None
 
     return DBNLogLikelihood
 
@@ -80,6 +89,29 @@ def shuffled_sessions(train: SessionSet, seed: int = 0) -> SessionSet:
     return SessionSet(train.query[perm], train.docs[perm], train.pidx[perm], train.click[perm])
 
 
+def query_order(train: SessionSet, seed: int = 0):
+    """The training sessions grouped by query, the queries in a random order,
+    with query-document indices renumbered in that order (the layout ingest
+    gives sessions sorted by query).  Returns (sessions, n_qd, to_original):
+    to_original[i] is the original index of renumbered pair i."""
+    from .api import Dataset
+    q = np.ascontiguousarray(train.query, np.int64)
+    uq, inv = np.unique(q, return_inverse=True)
+    perm = np.random.default_rng(seed).permutation(len(uq))
+    relabel = perm[inv].astype(np.int32)       # a random rank for every query
+    ds = Dataset.from_sessions(relabel, train.docs, train.click, 0.0)
+    # pair key (query, doc) -> original index, looked up for the new indices
+    orig_q = uq[np.argsort(perm)][ds.train.query.astype(np.int64)]
+    key_new = (orig_q[:, None] << 32) | ds.train.docs.astype(np.int64)
+    key_old = (q[:, None] << 32) | train.docs.astype(np.int64)
+    ko, first = np.unique(key_old.ravel(), return_index=True)
+    old_idx = train.pidx.ravel()[first]
+    pos = np.searchsorted(ko, key_new.ravel())
+    to_original = np.empty(ds.n_qd, np.int64)
+    to_original[ds.train.pidx.ravel()] = old_idx[pos]
+    return ds.train, ds.n_qd, to_original
+
+
 def logits_to_values(alpha, beta, gamma) -> dict:
     import torch
     return {"attractiveness": torch.sigmoid(alpha).detach().cpu().numpy(),
@@ -90,8 +122,11 @@ def logits_to_values(alpha, beta, gamma) -> dict:
 def train_adam(model: ClickModel, n_qd: int, steps: int, batch: int = 262144, lr: float = 0.05,
                callback=None, callback_every: int = 0, device: int = 0):
     """Adam on the logits, minibatches of `batch` consecutive sessions of the
-    model's (shuffled) training set, loss = -log-likelihood / batch.  The
-    callback gets (step, seconds, alpha, beta, gamma) every callback_every steps."""
+    model's training set (lay it out with query_order or shuffle it for
+    unbiased batches), loss = -log-likelihood / batch.  Every callback_every
+    steps the device is synchronised and callback(step, seconds, alpha, beta,
+    gamma) runs; `seconds` is the training time so far, and the callback's own
+    time is not counted.  No step waits for the host otherwise."""
     import torch
     dev = torch.device("cuda", device)
     alpha = torch.zeros(n_qd, dtype=torch.float32, device=dev, requires_grad=True)
@@ -99,6 +134,8 @@ def train_adam(model: ClickModel, n_qd: int, steps: int, batch: int = 262144, lr
     gamma = torch.zeros(1, dtype=torch.float32, device=dev, requires_grad=True)
     opt = torch.optim.Adam([alpha, beta, gamma], lr=lr)
     n = model.n_train
+    torch.cuda.synchronize(dev)
+    elapsed = 0.0
     t0 = time.perf_counter()
     begin = 0
     for step in range(steps):
@@ -109,6 +146,9 @@ def train_adam(model: ClickModel, n_qd: int, steps: int, batch: int = 262144, lr
         opt.step()
         begin = begin + count if begin + count < n else 0
         if callback and callback_every and (step + 1) % callback_every == 0:
-            torch.cuda.synchronize()
-            callback(step + 1, time.perf_counter() - t0, alpha, beta, gamma)
+            torch.cuda.synchronize(dev)
+            elapsed += time.perf_counter() - t0
+            callback(step + 1, elapsed, alpha, beta, gamma)
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
     return alpha, beta, gamma

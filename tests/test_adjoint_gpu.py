@@ -46,23 +46,23 @@ def test_forward_matches_oracle():
     assert ll32 == pytest.approx(ref, rel=1e-6)
 
 
-def test_gradient_matches_central_differences():
-    """1,000 random parameters against FP64 central differences with step
-    1e-4 (truncation error about 1e-8 relative).  A pair's difference is taken
-    over the sessions that show it: the other sessions' terms are identical
-    on both sides, and leaving them in would only add the rounding noise of a
-    10^4-sized sum (about 1e-6 absolute after dividing by 2h)."""
-    case, cm, al, be, ga = _setup(seed=1)
-    _, ga_, gb_, gg_ = _grads(cm, al, be, ga, True)
+def _fd_errors(case, al, be, ga, ga_, gb_, gg_, seed=2):
+    """Relative errors of a gradient against FP64 central differences of the
+    oracle's likelihood (step 1e-4, truncation error about 1e-8 relative) on
+    1,000 random parameters.  A pair's difference is taken over the sessions
+    that show it: the other sessions' terms are identical on both sides, and
+    leaving them in would only add the rounding noise of a 10^4-sized sum
+    (about 1e-6 absolute after dividing by 2h).  Parameters whose gradient is
+    about 0 compare absolutely (denominator at least 1e-3)."""
     p, m = case["train_pidx"], case["train_click"]
     A, B = al.astype(np.float64), be.astype(np.float64)
     G = float(ga[0])
     h = 1e-4
-    rng = np.random.default_rng(2)
+    rng = np.random.default_rng(seed)
     n_qd = A.shape[0]
     picks = [("a", int(i)) for i in rng.choice(n_qd, 600, replace=False)] + \
             [("b", int(i)) for i in rng.choice(n_qd, 399, replace=False)] + [("g", 0)]
-    worst = 0.0
+    errs = []
     for kind, i in picks:
         if kind in ("a", "b"):
             rows = np.any(p == i, axis=1)
@@ -80,11 +80,58 @@ def test_gradient_matches_central_differences():
         else:
             fd = (bindings.dbn_loglik(p, m, A, B, G + h) - bindings.dbn_loglik(p, m, A, B, G - h)) / (2 * h)
             got = gg_
-        # relative 1e-6; parameters whose gradient is ~0 (never affect the
-        # likelihood) compare absolutely
-        err = abs(got - fd) / max(abs(fd), 1e-3)
-        worst = max(worst, err)
+        errs.append(abs(got - fd) / max(abs(fd), 1e-3))
+    return np.array(errs)
+
+
+def test_gradient_matches_central_differences():
+    """The FP64 instantiation within 1e-6 relative of the differences."""
+    case, cm, al, be, ga = _setup(seed=1)
+    _, ga_, gb_, gg_ = _grads(cm, al, be, ga, True)
+    worst = _fd_errors(case, al, be, ga, ga_, gb_, gg_).max()
     assert worst <= 1e-6, worst
+
+
+def test_fp32_gradient_matches_central_differences():
+    """The FP32 gradient the trainer uses, against the same FP64 differences:
+    within 1e-4 relative.  Adam divides each step by the root of a running
+    second moment, so the step direction needs a few significant digits; the
+    bar is 100 times tighter than the 1e-2 at which Adam's steps would change
+    visibly."""
+    case, cm, al, be, ga = _setup(seed=1)
+    _, ga_, gb_, gg_ = _grads(cm, al, be, ga, False)
+    worst = _fd_errors(case, al, be, ga, ga_, gb_, gg_).max()
+    assert worst <= 1e-4, worst
+
+
+def test_tile_path_matches_session_path():
+    """A model whose sessions are grouped by query takes the tile path (the
+    gradient summed per tile in shared memory); the same sessions in random
+    order take one thread per session with global atomics.  Both give the
+    same log-likelihood and gradient, also over partial ranges."""
+    case, cm, al, be, ga = _setup("dbn_ccmclicks", seed=6)
+    train = api.SessionSet(case["train_query"], case["train_docs"], case["train_pidx"], case["train_click"])
+    shuffled = gradient.shuffled_sessions(train, seed=3)
+    cm2 = api.DBNModel()
+    cm2.upload(shuffled, int(case["n_qd"]))
+    for fp64 in (True, False):
+        l1, a1, b1, g1 = _grads(cm, al, be, ga, fp64)
+        l2, a2, b2, g2 = _grads(cm2, al, be, ga, fp64)
+        tol = 1e-9 if fp64 else 2e-5
+        assert l1 == pytest.approx(l2, rel=tol)
+        np.testing.assert_allclose(a1, a2, rtol=tol, atol=tol)
+        np.testing.assert_allclose(b1, b2, rtol=tol, atol=tol)
+        assert g1 == pytest.approx(g2, rel=tol)
+    # a range that starts and ends inside tiles, against the oracle
+    dev = torch.device("cuda", 0)
+    lo, hi = 777, cm.n_train - 555
+    a = torch.tensor(al, device=dev, requires_grad=True)
+    b = torch.tensor(be, device=dev, requires_grad=True)
+    g = torch.tensor(ga, device=dev, requires_grad=True)
+    ll = gradient.dbn_loglik(a, b, g, cm, lo, hi - lo, fp64=True)
+    ref = bindings.dbn_loglik(case["train_pidx"][lo:hi], case["train_click"][lo:hi], al.astype(np.float64),
+                              be.astype(np.float64), float(ga[0]))
+    assert float(ll.detach()) == pytest.approx(ref, rel=1e-12)
 
 
 def test_gradient_equals_fisher_scores():
