@@ -553,7 +553,7 @@ def run_batched(args, rank: int, world: int, local: int):
     n_fits, n_tiles, _ = batch.info()
     n_count_fits = sum(1 for cm in models if cm.fused_path()[0] in ("counts", "dense"))
     # per iteration: the tile launch (DBN/CCM fits) and the batched count launch (PBM/UBM fits)
-    launches_per_iteration = int(n_tiles > 0) + int(n_count_fits > 0)
+    launches_per_iteration = batch.launches_per_iteration()
 
     def timed(fn, steps):
         torch.cuda.synchronize()
@@ -570,6 +570,11 @@ def run_batched(args, rank: int, world: int, local: int):
     clocks.start()
     ms_batch = timed(lambda k: batch.em(k, stream), args.steps)
     clk = clocks.stop()
+    # the same iterations with the count chunks taken by the tile launch itself
+    batch.configure(True)
+    batch.em(args.warmup, stream)
+    ms_single = timed(lambda k: batch.em(k, stream), max(1, args.steps // 4))
+    batch.configure(False)
     for cm in models:
         cm.em(1, IMPL_FUSED, stream)
     ms_sep = timed(lambda k: [cm.em(k, IMPL_FUSED, stream) for cm in models], max(1, args.steps // 4))
@@ -587,6 +592,8 @@ def run_batched(args, rank: int, world: int, local: int):
             "config": {"workload": f"{n_fits} fits, {int(sizes.sum())} sessions ({n_train} training), per iteration "
                                    "one tile launch for the DBN fits and one count launch for the PBM/UBM fits",
                        "tiles": n_tiles, "count_path_fits": n_count_fits, "prep_s": round(prep_s, 2)},
+            "single_launch": {"value": n_train / (ms_single / 1000.0), "ms_per_step": ms_single,
+                              "note": "count chunks taken by the persistent tile launch after its tiles"},
             "separate_fused": {"value": n_train / (ms_sep / 1000.0), "ms_per_step": ms_sep},
             "separate_plain": {"value": n_train / (ms_plain / 1000.0), "ms_per_step": ms_plain,
                                "batched_speedup": ms_plain / ms_batch},

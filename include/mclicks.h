@@ -157,10 +157,20 @@ int mc_model_init_parameters(mc_model* m, void* stream);
 int mc_model_configure(mc_model* m, int32_t sessions_per_tile, int32_t window_qd, int32_t block_size);
 int mc_model_get_config(const mc_model* m, int32_t* sessions_per_tile, int32_t* window_qd, int32_t* block_size);
 
-/* Times a few fused iterations for each tile shape of a small grid and keeps
- * the fastest.  Parameters are restored afterwards.  A model on the count path
- * (mc_model_fused_path: PBM, UBM) has no tile shape to tune and returns at once. */
+/* Times a few fused iterations for each candidate shape and keeps the
+ * fastest: the tile shape (sessions per tile, window, block) on the tile
+ * path; on the count path (mc_model_fused_path: PBM, UBM) the count kernel's
+ * bin copies, block size and blocks per SM.  Parameters are restored
+ * afterwards.  (No counterpart in the reference, whose launches are fixed at
+ * BLOCK_SIZE threads, utils/definitions.h.) */
 int mc_model_autotune(mc_model* m, void* stream);
+
+/* Launch shape of the count-path kernels (no counterpart in the reference):
+ * copies of each warp's public bins (4, 8 or 16; ignored by the dense PBM
+ * kernel), threads per block (a multiple of 32 in [64, 256]) and blocks per
+ * SM of the grid.  Results do not depend on the shape. */
+int mc_model_configure_counts(mc_model* m, int32_t copies, int32_t block, int32_t blocks_per_sm);
+int mc_model_get_count_config(const mc_model* m, int32_t* copies, int32_t* block, int32_t* blocks_per_sm);
 
 /* Runs n_iterations EM iterations: replaces the loop of em_parallel
  * (parallel_em/parallel_em.cu:462-609): Kernel::em_training, reset_parameters,
@@ -268,6 +278,19 @@ int mc_batch_em(mc_batch* b, int32_t n_iterations, void* stream);
 /* n_tiles: tiles of the tile launch; mixed_models: its tile fits are of more
  * than one model type (the model-generic kernel runs). */
 int mc_batch_info(const mc_batch* b, int32_t* n_models, int32_t* n_tiles, int32_t* mixed_models);
+
+/* How a batch with both kinds of fit runs an iteration (no counterpart in the
+ * reference, which runs one model per process, parallel_em.cu:364-372):
+ * single_launch = 1 makes the persistent tile launch take the count chunks of
+ * the count-path fits (PBM, UBM) after its tiles, one launch per iteration;
+ * 0 (the default) follows the tile launch with a count launch.  The default
+ * is the faster on the 256-fit benchmark (0.34 against 0.40 ms per
+ * iteration): the count kernel runs three times the warps per SM that the
+ * tile kernel's two CTAs hold.  Results are the same either way. */
+int mc_batch_configure(mc_batch* b, int single_launch);
+
+/* Kernel launches one iteration of the batch makes (0, 1 or 2). */
+int mc_batch_launches(const mc_batch* b, int32_t* launches_per_iteration);
 
 void mc_batch_destroy(mc_batch* b);
 

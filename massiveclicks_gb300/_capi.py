@@ -49,6 +49,8 @@ _SIGS = {
     "mc_model_configure": (C.c_int, [_VP, _I32, _I32, _I32]),
     "mc_model_get_config": (C.c_int, [_VP, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32)]),
     "mc_model_autotune": (C.c_int, [_VP, _VP]),
+    "mc_model_configure_counts": (C.c_int, [_VP, _I32, _I32, _I32]),
+    "mc_model_get_count_config": (C.c_int, [_VP, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32)]),
     "mc_model_em": (C.c_int, [_VP, _I32, C.c_int, _VP]),
     "mc_model_process_sessions": (C.c_int, [_VP, _VP]),
     "mc_model_update_parameters": (C.c_int, [_VP, _VP]),
@@ -67,6 +69,8 @@ _SIGS = {
     "mc_batch_create": (C.c_int, [C.c_int, _VP, C.POINTER(_VP)]),
     "mc_batch_em": (C.c_int, [_VP, _I32, _VP]),
     "mc_batch_info": (C.c_int, [_VP, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32)]),
+    "mc_batch_launches": (C.c_int, [_VP, C.POINTER(_I32)]),
+    "mc_batch_configure": (C.c_int, [_VP, C.c_int]),
     "mc_batch_destroy": (None, [_VP]),
     "mc_dbn_loglik_forward": (C.c_int, [_VP, _I64, _I64, _VP, _VP, _VP, C.c_int, C.POINTER(_F64), _VP]),
     "mc_dbn_loglik_backward": (C.c_int, [_VP, _I64, _I64, _VP, _VP, _VP, C.c_int, _F64, _VP, _VP, _VP,

@@ -205,6 +205,15 @@ class ClickModel:
         return self.get_config()
 
     # -- EM -------------------------------------------------------------------------
+    def configure_counts(self, copies: int, block: int, blocks_per_sm: int) -> None:
+        """Launch shape of the count-path kernels (PBM, UBM)."""
+        check(_capi.load().mc_model_configure_counts(self._h, int(copies), int(block), int(blocks_per_sm)))
+
+    def count_config(self) -> tuple[int, int, int]:
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        check(_capi.load().mc_model_get_count_config(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
     def em(self, iterations: int, impl: int = IMPL_FUSED, stream=None) -> None:
         check(_capi.load().mc_model_em(self._h, int(iterations), int(impl), _stream(stream)))
 
@@ -324,6 +333,15 @@ class Batch:
         a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
         check(_capi.load().mc_batch_info(self._h, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, bool(c.value)
+
+    def configure(self, single_launch: bool) -> None:
+        """single_launch: the tile launch takes the count fits' chunks too."""
+        check(_capi.load().mc_batch_configure(self._h, int(bool(single_launch))))
+
+    def launches_per_iteration(self) -> int:
+        n = C.c_int32()
+        check(_capi.load().mc_batch_launches(self._h, C.byref(n)))
+        return n.value
 
     def close(self) -> None:
         if self._h:

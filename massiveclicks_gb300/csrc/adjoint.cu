@@ -116,14 +116,27 @@ __global__ void __launch_bounds__(256) adjoint_kernel(AdjointArgs A, bool grad) 
 // chunk of a split query.  A wider window takes the per-session kernel's
 // global atomics.  The continuation gradient and the log-likelihood go
 // through registers and one FP64 atomic per block.
+// A window of at most kSmallWin pairs (a head query's chunk: a few dozen
+// documents shown to thousands of sessions) sums into kSmallCopies copies of
+// its bins, one per (warp, lane % 4), so that only lanes of one warp with the
+// same lane % 4 meet on an address; the copies are added at the flush.
+constexpr int kSmallWin = 64;
+constexpr int kSmallCopies = 32;
+
+template <typename T>
+__host__ __device__ constexpr int adjoint_smem_elems(int window_max) {
+    return 4 * window_max > 2 * kSmallWin + 2 * kSmallWin * kSmallCopies ? 4 * window_max
+                                                                        : 2 * kSmallWin + 2 * kSmallWin * kSmallCopies;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) adjoint_tiles_kernel(AdjointArgs A, const TileDev* __restrict__ tiles, int t0,
                                                            int t1, int window_max, bool grad) {
     extern __shared__ __align__(16) unsigned char sm[];
-    T* va = reinterpret_cast<T*>(sm);             // [window_max] attractiveness of the window
-    T* vs = va + window_max;                       // [window_max] satisfaction
-    T* ga = vs + window_max;                       // [window_max] gradient sums (alpha)
-    T* gb = ga + window_max;                       // [window_max] gradient sums (beta)
+    // Wide window: va, vs, ga, gb of window_max entries each.  Small window
+    // (<= kSmallWin): va, vs of kSmallWin entries, then the copies
+    // [kSmallCopies][2][kSmallWin] (alpha, beta).
+    T* const base = reinterpret_cast<T*>(sm);
     __shared__ double red[2][8];
     const T g = sigm<T>(A.gamma[0]);
     const T w = (T)A.scale;
@@ -136,13 +149,22 @@ __global__ void __launch_bounds__(256) adjoint_tiles_kernel(AdjointArgs A, const
         const int64_t s1 = tile.s_begin + tile.s_count < r1 ? tile.s_begin + tile.s_count : r1;
         if (s0 >= s1) continue;  // uniform over the block
         const bool staged = tile.qd_count <= window_max;
+        const bool small = staged && tile.qd_count <= kSmallWin;
+        const int wcap = small ? kSmallWin : window_max;
+        T* const va = base;
+        T* const vs = base + wcap;
+        T* const ga = base + 2 * wcap;             // wide window only
+        T* const gb = base + 3 * wcap;
+        T* const cp = base + 2 * kSmallWin;        // small window: the copies
+        T* const my = cp + ((threadIdx.x >> 5) * 4 + (threadIdx.x & 3)) * 2 * kSmallWin;
         if (staged) {
             for (int i = threadIdx.x; i < tile.qd_count; i += blockDim.x) {
                 va[i] = sigm<T>(A.alpha[tile.qd_begin + i]);
                 vs[i] = sigm<T>(A.beta[tile.qd_begin + i]);
-                ga[i] = T(0);
-                gb[i] = T(0);
+                if (!small) { ga[i] = T(0); gb[i] = T(0); }
             }
+            if (small)
+                for (int i = threadIdx.x; i < 2 * kSmallWin * kSmallCopies; i += blockDim.x) cp[i] = T(0);
             __syncthreads();
         }
         for (int64_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
@@ -183,7 +205,8 @@ __global__ void __launch_bounds__(256) adjoint_tiles_kernel(AdjointArgs A, const
                     ex_bar = T(1) / ex[r];
                     g_bar_acc += e_bar * (T(1) - sv[r]);
                     const T db = w * (-e_bar * g) * sv[r] * (T(1) - sv[r]);
-                    if (staged) atomicAdd(gb + rl[r], db);
+                    if (small) atomicAdd(my + kSmallWin + rl[r], db);
+                    else if (staged) atomicAdd(gb + rl[r], db);
                     else atomicAdd(A.g_beta + rl[r], (double)db);
                 } else {
                     const T ip = T(1) / pr[r];
@@ -192,7 +215,8 @@ __global__ void __launch_bounds__(256) adjoint_tiles_kernel(AdjointArgs A, const
                     g_bar_acc += e_bar * ex[r] * (T(1) - a[r]) * ip;
                 }
                 const T da = w * a_bar * a[r] * (T(1) - a[r]);
-                if (staged) atomicAdd(ga + rl[r], da);
+                if (small) atomicAdd(my + rl[r], da);
+                else if (staged) atomicAdd(ga + rl[r], da);
                 else atomicAdd(A.g_alpha + rl[r], (double)da);
                 e_bar = ex_bar;
             }
@@ -203,12 +227,24 @@ __global__ void __launch_bounds__(256) adjoint_tiles_kernel(AdjointArgs A, const
                 const bool owned = tile.split < 0;
                 for (int i = threadIdx.x; i < tile.qd_count; i += blockDim.x) {
                     const int64_t q = tile.qd_begin + i;
-                    if (owned) {
-                        A.g_alpha[q] = (double)ga[i];
-                        A.g_beta[q] = (double)gb[i];
+                    double sa, sb;
+                    if (small) {
+                        sa = 0.0;
+                        sb = 0.0;
+                        for (int c = 0; c < kSmallCopies; c++) {
+                            sa += (double)cp[c * 2 * kSmallWin + i];
+                            sb += (double)cp[c * 2 * kSmallWin + kSmallWin + i];
+                        }
                     } else {
-                        if (ga[i] != T(0)) atomicAdd(A.g_alpha + q, (double)ga[i]);
-                        if (gb[i] != T(0)) atomicAdd(A.g_beta + q, (double)gb[i]);
+                        sa = (double)ga[i];
+                        sb = (double)gb[i];
+                    }
+                    if (owned) {
+                        A.g_alpha[q] = sa;
+                        A.g_beta[q] = sb;
+                    } else {
+                        if (sa != 0.0) atomicAdd(A.g_alpha + q, sa);
+                        if (sb != 0.0) atomicAdd(A.g_beta + q, sb);
                     }
                 }
             }
@@ -242,7 +278,9 @@ cudaError_t launch_adjoint(const AdjointArgs& A, bool grad, bool fp64, int n_sm,
     return cudaGetLastError();
 }
 
-size_t adjoint_tiles_smem(int window_max, bool fp64) { return (size_t)4 * window_max * (fp64 ? 8 : 4); }
+size_t adjoint_tiles_smem(int window_max, bool fp64) {
+    return (size_t)adjoint_smem_elems<float>(window_max) * (fp64 ? 8 : 4);
+}
 
 cudaError_t launch_adjoint_tiles(const AdjointArgs& A, const TileDev* tiles, int t0, int t1, int window_max, bool grad,
                                  bool fp64, int n_sm, cudaStream_t st) {

@@ -92,6 +92,8 @@ struct SplitDev {
 struct WorkState {
     unsigned next_tile;
     unsigned ctas_exited;
+    unsigned next_count;   // count chunks of batched count-path fits taken so far
+    unsigned pad_;
 };
 
 // Counters of the upload pass beyond the UBM slot counts.

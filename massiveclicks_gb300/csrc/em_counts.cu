@@ -22,8 +22,11 @@
 #include <cuda_runtime.h>
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_run_length_encode.cuh>
+#include <cub/device/device_scan.cuh>
+#include <thrust/iterator/reverse_iterator.h>
 
 #include "common.cuh"
+#include "count_step.cuh"
 #include "devmem.h"
 #include "kernels.h"
 
@@ -75,20 +78,22 @@ __global__ void count_entries_kernel(int64_t runs, const K* __restrict__ uniq, c
     }
 }
 
-// off[q] = first run whose qd is >= q, for q in [0, n_qd]: run i writes the
-// offsets from just after the previous run's qd up to its own qd, and the last
-// run also those after its qd.  (off starts zeroed, which covers no runs.)
+// off[q] = first run whose qd is >= q, for q in [0, n_qd], in two parallel
+// steps: the first run of each qd writes its index at off[qd] (the others
+// hold ~0, off[n_qd] = runs), then a suffix minimum fills each gap with the
+// next qd's value.
 template <class K>
-__global__ void count_offsets_kernel(int64_t n_qd, int64_t runs, const K* __restrict__ uniq, uint32_t* __restrict__ off) {
+__global__ void count_first_run_kernel(int64_t runs, const K* __restrict__ uniq, uint32_t* __restrict__ off) {
     const int64_t step = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < runs; i += step) {
         const int64_t q = (int64_t)(uniq[i] >> 7);
-        const int64_t qp = i ? (int64_t)(uniq[i - 1] >> 7) : -1;
-        for (int64_t x = qp + 1; x <= q; x++) off[x] = (uint32_t)i;
-        if (i == runs - 1)
-            for (int64_t x = q + 1; x <= n_qd; x++) off[x] = (uint32_t)runs;
+        if (i == 0 || (int64_t)(uniq[i - 1] >> 7) != q) off[q] = (uint32_t)i;
     }
 }
+
+struct MinU32 {
+    __device__ __forceinline__ uint32_t operator()(uint32_t a, uint32_t b) const { return a < b ? a : b; }
+};
 
 // PBM: dense[qd * 10 + rank] = count of run i (every PBM key is alive and
 // unique per (qd, rank)); flags a count above 65535.
@@ -167,16 +172,31 @@ static cudaError_t build_counts_t(int model, int64_t n, int64_t stride, int64_t 
         ck(cudaMemcpy(&last_key, uniq + runs - 1, sizeof(K), cudaMemcpyDeviceToHost));
         if (last_key == ~K(0)) runs--;
     }
+    const uint32_t runs32 = (uint32_t)runs;  // < 2^32: n * 10 < 2^32 entries at most
     ck(tmp_alloc(&off, (size_t)n_qd + 1));
     ck(tmp_alloc(&ent, (size_t)(runs > 0 ? runs : 1)));
     if (model == PBM && dense_out) ck(tmp_alloc(&dense, (size_t)n_qd * MC_R));
     int* overflow = reinterpret_cast<int*>(d_small + 1);
     if (e == cudaSuccess) {
-        ck(cudaMemsetAsync(off, 0, ((size_t)n_qd + 1) * sizeof(uint32_t), st));
+        ck(cudaMemsetAsync(off, 0xFF, (size_t)n_qd * sizeof(uint32_t), st));
+        ck(cudaMemcpyAsync(off + n_qd, &runs32, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
         count_entries_kernel<K><<<grid_for(runs, n_sm), 256, 0, st>>>(runs, uniq, counts, ent, overflow);
         ck(cudaGetLastError());
-        count_offsets_kernel<K><<<grid_for(runs, n_sm), 256, 0, st>>>(n_qd, runs, uniq, off);
+        count_first_run_kernel<K><<<grid_for(runs, n_sm), 256, 0, st>>>(runs, uniq, off);
         ck(cudaGetLastError());
+        {
+            auto rev = thrust::make_reverse_iterator(off + n_qd + 1);
+            size_t scan_bytes = 0;
+            ck(cub::DeviceScan::InclusiveScan(nullptr, scan_bytes, rev, rev, MinU32(), (int64_t)n_qd + 1, st));
+            void* scan_tmp = nullptr;
+            ck(mch::dev_alloc(&scan_tmp, scan_bytes ? scan_bytes : 1));
+            if (e == cudaSuccess)
+                ck(cub::DeviceScan::InclusiveScan(scan_tmp, scan_bytes, rev, rev, MinU32(), (int64_t)n_qd + 1, st));
+            if (scan_tmp) {
+                cudaStreamSynchronize(st);
+                mch::dev_free(scan_tmp);
+            }
+        }
         if (dense) {
             ck(cudaMemsetAsync(dense, 0, (size_t)n_qd * MC_R * sizeof(uint16_t), st));
             count_dense_kernel<K><<<grid_for(runs, n_sm), 256, 0, st>>>(runs, uniq, counts, dense, overflow + 1);
@@ -227,99 +247,48 @@ cudaError_t build_counts(int model, int64_t n, int64_t stride, int64_t n_qd, con
 // all slower at 22.6M qd: the kernel is bound by the shared-memory pipe and
 // lane divergence, not by DRAM latency.)
 //
-// After a block has added its public partial sums: the last of the fit's
-// n_blocks blocks to finish runs the public M-step into the other half of the
-// double buffer, clears the bins and the block counter and advances iter.
-__device__ __forceinline__ void public_finish(const FitDev& f, int s_it, unsigned n_blocks) {
-    __shared__ int s_last;
-    const int tid = threadIdx.x;
-    const int n_pub = f.n_pub;
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) s_last = atomicAdd(f.tiles_done, 1u) + 1 == n_blocks;
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    const int nb = (s_it + 1) & 1;
-    if (tid < n_pub) {
-        const double num = f.pub_const[2 * tid] + __ldcg(f.pub_bins + 2 * tid);
-        const double den = f.pub_const[2 * tid + 1] + __ldcg(f.pub_bins + 2 * tid + 1);
-        const double v = num / den;
-        f.pub_theta[nb * MC_MAX_PUB + tid] = (float)(v < (double)MC_TOP ? v : (double)MC_TOP);
-        f.pub_bins[2 * tid] = 0.0;
-        f.pub_bins[2 * tid + 1] = 0.0;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        *f.tiles_done = 0;
-        __threadfence();
-        *(volatile int*)f.iter = s_it + 1;
-    }
-}
-
-// The block takes qd q_first, q_first + q_step, ... below q_end; the fit's
-// iteration is done by n_blocks blocks, and the last of them to finish runs
-// the public M-step.  COPIES copies of each warp's public bins: lane l adds
-// to copy l % COPIES, so only lanes that share a copy and a key meet on one
-// shared-memory address.
+// One block's share of an iteration: count_step (count_step.cuh) over static
+// shared memory.
 template <int COPIES>
 __device__ __forceinline__ void count_iteration(const FitDev& f, const uint32_t* __restrict__ off,
                                                 const uint32_t* __restrict__ ent, int64_t q_first, int64_t q_end,
                                                 int64_t q_step, unsigned n_blocks) {
-    constexpr int kBinCopies = COPIES;
-    __shared__ float e[64];
-    __shared__ float wbin[8][MC_UBM_SLOTS][kBinCopies];
-    __shared__ int s_it;
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const int n_pub = f.n_pub;
-    if (tid == 0) s_it = *(volatile int*)f.iter;
-    for (int k = tid; k < 8 * MC_UBM_SLOTS * kBinCopies; k += blockDim.x) (&wbin[0][0][0])[k] = 0.0f;
-    __syncthreads();
-    if (tid < 64) e[tid] = tid < n_pub ? f.pub_theta[(s_it & 1) * MC_MAX_PUB + tid] : 0.0f;
-    __syncthreads();
-    float* mybin = &wbin[warp][0][tid & (kBinCopies - 1)];
-    for (int64_t q = q_first; q < q_end; q += q_step) {
-        const float a = f.atr[q];
-        const uint2 c = f.cnt[q];
-        const uint32_t i1 = __ldg(off + q + 1);
-        float v0 = 0.0f;
-        for (uint32_t i = __ldg(off + q); i < i1; i++) {
-            const uint32_t x = __ldg(ent + i);
-            const int k = (int)((x >> 1) & 63u);
-            const float ek = e[k];
-            const float ae = a * ek;
-            const float w = (float)(x >> 7) * __fdividef(1.0f, 1.0f - ae);
-            v0 += w * (a - ae);
-            if (x & 1u) atomicAdd(mybin + k * kBinCopies, w * (ek - ae));
-        }
-        // M-step, PBM and UBM in both modes: (1 + clicks + v0) / (2 + occurrences).
-        const float v = __fdividef(1.0f + (float)c.y + v0, 2.0f + (float)c.x);
-        f.atr[q] = v < MC_TOP ? v : MC_TOP;
-    }
-    __syncthreads();
-    if (tid < n_pub) {
-        double s = 0.0;
-        for (int w = 0; w < 8; w++)
-            for (int c = 0; c < kBinCopies; c++) s += (double)wbin[w][tid][c];
-        if (s != 0.0) atomicAdd(f.pub_bins + 2 * tid, s);
-    }
-    public_finish(f, s_it, n_blocks);
+    __shared__ __align__(16) float sm[count_step_smem<COPIES>() / sizeof(float)];
+    __shared__ int s_int[2];
+    count_step<COPIES>(f, off, ent, q_first, q_end, q_step, n_blocks, sm, s_int);
 }
 
 // One fit: blocks stride over its qd.
-__global__ void __launch_bounds__(256, 8) em_counts_kernel(const FitDev* __restrict__ fp, const uint32_t* __restrict__ off,
-                                                           const uint32_t* __restrict__ ent) {
+template <int COPIES>
+__global__ void __launch_bounds__(256) em_counts_kernel(const FitDev* __restrict__ fp, const uint32_t* __restrict__ off,
+                                                        const uint32_t* __restrict__ ent) {
     const FitDev& f = *fp;
-    count_iteration<8>(f, off, ent, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, f.n_qd,
-                       (int64_t)gridDim.x * blockDim.x, gridDim.x);
+    count_iteration<COPIES>(f, off, ent, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, f.n_qd,
+                            (int64_t)gridDim.x * blockDim.x, gridDim.x);
+}
+
+// Grid of a grid-stride count launch: enough blocks for one qd per thread, at
+// most blocks_per_sm per SM.
+static int count_grid(int64_t n_qd, int block, int blocks_per_sm, int n_sm) {
+    const int64_t blocks = (n_qd + block - 1) / block;
+    const int64_t cap = (int64_t)blocks_per_sm * n_sm;
+    const int g = (int)(blocks < cap ? blocks : cap);
+    return g < 1 ? 1 : g;
+}
+
+bool count_shape_valid(const CountShape& c, bool dense) {
+    if (c.block < 64 || c.block > 256 || c.block % 32 || c.blocks_per_sm < 1 || c.blocks_per_sm > 32) return false;
+    return dense || c.copies == 4 || c.copies == 8 || c.copies == 16;
 }
 
 cudaError_t launch_em_counts(const FitDev* fit, const uint32_t* off, const uint32_t* ent, int64_t n_qd, int n_sm,
-                             cudaStream_t st) {
-    const int64_t blocks = (n_qd + 255) / 256;
-    int g = (int)(blocks < 8 * n_sm ? blocks : 8 * n_sm);
-    if (g < 1) g = 1;
-    em_counts_kernel<<<g, 256, 0, st>>>(fit, off, ent);
+                             const CountShape& c, cudaStream_t st) {
+    const int g = count_grid(n_qd, c.block, c.blocks_per_sm, n_sm);
+    switch (c.copies) {
+        case 4: em_counts_kernel<4><<<g, c.block, 0, st>>>(fit, off, ent); break;
+        case 16: em_counts_kernel<16><<<g, c.block, 0, st>>>(fit, off, ent); break;
+        default: em_counts_kernel<8><<<g, c.block, 0, st>>>(fit, off, ent); break;
+    }
     return cudaGetLastError();
 }
 
@@ -327,7 +296,7 @@ cudaError_t launch_em_counts(const FitDev* fit, const uint32_t* off, const uint3
 // ranks 0..9 (uint16), so every thread runs the same ten-rank loop and the
 // rank sums stay in registers (no shared atomics); warp sums, then FP64 block
 // sums, then one global atomic per rank per block.
-__global__ void __launch_bounds__(256, 6) em_counts_pbm_dense_kernel(const FitDev* __restrict__ fp,
+__global__ void __launch_bounds__(256) em_counts_pbm_dense_kernel(const FitDev* __restrict__ fp,
                                                                     const uint16_t* __restrict__ dense) {
     __shared__ float wsum[8][MC_R];
     __shared__ float e[MC_R];  // read with one address per warp (broadcast)
@@ -377,14 +346,13 @@ __global__ void __launch_bounds__(256, 6) em_counts_pbm_dense_kernel(const FitDe
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += (double)wsum[w][tid];
         if (s != 0.0) atomicAdd(f.pub_bins + 2 * tid, s);
     }
-    public_finish(f, s_it, gridDim.x);
+    __shared__ int s_last;
+    count_public_finish(f, s_it, gridDim.x, &s_last);
 }
 
-cudaError_t launch_em_counts_pbm_dense(const FitDev* fit, const uint16_t* dense, int64_t n_qd, int n_sm, cudaStream_t st) {
-    const int64_t blocks = (n_qd + 255) / 256;
-    int g = (int)(blocks < 6 * n_sm ? blocks : 6 * n_sm);
-    if (g < 1) g = 1;
-    em_counts_pbm_dense_kernel<<<g, 256, 0, st>>>(fit, dense);
+cudaError_t launch_em_counts_pbm_dense(const FitDev* fit, const uint16_t* dense, int64_t n_qd, int n_sm,
+                                       const CountShape& c, cudaStream_t st) {
+    em_counts_pbm_dense_kernel<<<count_grid(n_qd, c.block, c.blocks_per_sm, n_sm), c.block, 0, st>>>(fit, dense);
     return cudaGetLastError();
 }
 

@@ -58,6 +58,7 @@
 #include <cub/block/block_radix_sort.cuh>
 
 #include "common.cuh"
+#include "count_step.cuh"
 #include "kernels.h"
 
 namespace mcd {
@@ -605,7 +606,8 @@ constexpr int kMQ = 4;
 template <int MODEL>
 __global__ void __launch_bounds__(FUSED_THREADS, FUSED_MIN_CTAS)
 em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ tiles, int n_tiles,
-                const SplitDev* __restrict__ splits, WorkState* ws, int window_max, int spt, int n_stages) {
+                const SplitDev* __restrict__ splits, WorkState* ws, int window_max, int spt, int n_stages,
+                const CountFitDev* __restrict__ cfits, int n_cfits, int count_blocks) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ double pub_acc[MC_MAX_PUB];
     __shared__ float pub_tile[2][MC_MAX_PUB];
@@ -986,12 +988,46 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
         }
         if (cur_fit >= 0 && !*(volatile int*)&s_abort) flush_fit(s_fit[fs], cur_count);
     }
+
+    // ---------------- count chunks of batched PBM / UBM fits ---------------
+    // With the tile queue empty, the CTA takes chunks of kCountChunk pairs of
+    // the batch's count-path fits from a second queue (count_step), in the
+    // shared memory the stage ring and bins used: no copy is in flight once
+    // the tile loop has ended (every stage filled after the last tile holds
+    // no tile), and the last M-step ended with the loop's final barrier.
+    if (n_cfits > 0) {
+        __shared__ int s_cchunk, s_cfit, s_cint[2];
+        float* csm = reinterpret_cast<float*>(smem);
+        for (;;) {
+            __syncthreads();
+            if (tid == 0) {
+                const int c = *(volatile int*)&s_abort ? count_blocks : (int)atomicAdd(&ws->next_count, 1u);
+                s_cchunk = c;
+                if (c < count_blocks) {  // the fit owning chunk c: last with blk_begin <= c
+                    int lo = 0, hi = n_cfits - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) / 2;
+                        if (cfits[mid].blk_begin <= c) lo = mid; else hi = mid - 1;
+                    }
+                    s_cfit = lo;
+                }
+            }
+            __syncthreads();
+            const int c = s_cchunk;
+            if (c >= count_blocks) break;
+            const CountFitDev cf = cfits[s_cfit];
+            const int64_t q0 = (int64_t)(c - cf.blk_begin) * kCountChunk;
+            const int64_t q1 = q0 + kCountChunk < cf.n_qd ? q0 + kCountChunk : cf.n_qd;
+            count_step<16>(*cf.fit, cf.off, cf.ent, q0 + tid, q1, blockDim.x, (unsigned)cf.n_blocks, csm, s_cint);
+        }
+    }
     __syncthreads();
     if (tid == 0) {
         __threadfence();
         unsigned e = atomicAdd(&ws->ctas_exited, 1u);
         if (e == gridDim.x - 1) {
             ws->next_tile = 0;
+            ws->next_count = 0;
             ws->ctas_exited = 0;
         }
     }
@@ -1003,21 +1039,22 @@ cudaError_t set_wait_hooks(unsigned long long wait_limit_ns, int stall_tile) {
     return e;
 }
 
-size_t fused_smem_bytes(int model, int window_max, int spt, int n_stages) {
+size_t fused_smem_bytes(int model, int window_max, int spt, int n_stages, bool with_counts) {
     Layout L = make_layout(model, spt, window_max);
-    return (size_t)L.stage_off + (size_t)n_stages * L.stage_bytes;
+    const size_t tiles = (size_t)L.stage_off + (size_t)n_stages * L.stage_bytes;
+    return with_counts && tiles < count_step_smem<16>() ? count_step_smem<16>() : tiles;
 }
 
 cudaError_t launch_em_fused(int model, const FitDev* fits, const TileDev* tiles, int n_tiles, const SplitDev* splits,
                             WorkState* ws, int window_max, int spt, int n_stages, int grid, int block,
-                            cudaStream_t stream) {
-    size_t smem = fused_smem_bytes(model, window_max, spt, n_stages);
+                            const CountFitDev* cfits, int n_cfits, int count_blocks, cudaStream_t stream) {
+    size_t smem = fused_smem_bytes(model, window_max, spt, n_stages, n_cfits > 0);
     switch (model) {
-        case PBM: em_fused_kernel<PBM><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max, spt, n_stages); break;
-        case CCM: em_fused_kernel<CCM><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max, spt, n_stages); break;
-        case DBN: em_fused_kernel<DBN><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max, spt, n_stages); break;
-        case UBM: em_fused_kernel<UBM><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max, spt, n_stages); break;
-        default: em_fused_kernel<-1><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max, spt, n_stages); break;
+        case PBM: em_fused_kernel<PBM><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max, spt, n_stages, cfits, n_cfits, count_blocks); break;
+        case CCM: em_fused_kernel<CCM><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max, spt, n_stages, cfits, n_cfits, count_blocks); break;
+        case DBN: em_fused_kernel<DBN><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max, spt, n_stages, cfits, n_cfits, count_blocks); break;
+        case UBM: em_fused_kernel<UBM><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max, spt, n_stages, cfits, n_cfits, count_blocks); break;
+        default: em_fused_kernel<-1><<<grid, block, smem, stream>>>(fits, tiles, n_tiles, splits, ws, window_max, spt, n_stages, cfits, n_cfits, count_blocks); break;
     }
     return cudaGetLastError();
 }

@@ -10,15 +10,20 @@
 namespace mcd {
 
 // ---- fused EM (em_fused.cu) -------------------------------------------------
-size_t fused_smem_bytes(int model, int window_max, int spt, int n_stages);
+struct CountFitDev;
+// Dynamic shared memory of the tile kernel; with_counts: enough for the count
+// chunks of batched count-path fits as well.
+size_t fused_smem_bytes(int model, int window_max, int spt, int n_stages, bool with_counts = false);
 cudaError_t fused_set_smem_limits(size_t bytes);
 cudaError_t fused_occupancy(int model, int block, size_t smem, int* blocks_per_sm);
 // Wait limit of the fused kernel's mbarrier waits and a tile whose stage is
 // made to stall (-1: none), on the current device; for the timeout tests.
 cudaError_t set_wait_hooks(unsigned long long wait_limit_ns, int stall_tile);
+// cfits / n_cfits / count_blocks: count-path fits of a batch whose chunks the
+// same launch takes after the tiles (nullptr, 0, 0 for none).
 cudaError_t launch_em_fused(int model, const FitDev* fits, const TileDev* tiles, int n_tiles, const SplitDev* splits,
                             WorkState* ws, int window_max, int spt, int n_stages, int grid, int block,
-                            cudaStream_t stream);
+                            const CountFitDev* cfits, int n_cfits, int count_blocks, cudaStream_t stream);
 // PBM/UBM iterations from counts per (qd, statistic key) (em_counts.cu).
 // build_counts sorts the unclicked occurrences of the uploaded sessions into
 // per-qd entries (CSR: off[n_qd + 1], ent[n_entries]); *usable = 0 keeps the
@@ -28,9 +33,17 @@ cudaError_t launch_em_fused(int model, const FitDev* fits, const TileDev* tiles,
 cudaError_t build_counts(int model, int64_t n, int64_t stride, int64_t n_qd, const int32_t* planes, const uint16_t* click,
                          int n_sm, cudaStream_t st, uint32_t** off, uint32_t** ent, int64_t* n_entries,
                          uint16_t** dense, int* usable);
-cudaError_t launch_em_counts_pbm_dense(const FitDev* fit, const uint16_t* dense, int64_t n_qd, int n_sm, cudaStream_t st);
+// Launch shape of the one-fit count kernels: copies of each warp's public
+// bins (4, 8 or 16; the entry kernel), threads per block (64..256, a multiple
+// of 32) and the most blocks per SM of the grid-stride grid.
+struct CountShape {
+    int copies, block, blocks_per_sm;
+};
+bool count_shape_valid(const CountShape& c, bool dense);
+cudaError_t launch_em_counts_pbm_dense(const FitDev* fit, const uint16_t* dense, int64_t n_qd, int n_sm,
+                                       const CountShape& c, cudaStream_t st);
 cudaError_t launch_em_counts(const FitDev* fit, const uint32_t* off, const uint32_t* ent, int64_t n_qd, int n_sm,
-                             cudaStream_t st);
+                             const CountShape& c, cudaStream_t st);
 // Batched count path: fit i takes blocks [blk_begin, blk_begin + n_blocks),
 // one chunk of kCountChunk qd each (n_blocks = ceil(n_qd / kCountChunk)).
 constexpr int kCountChunk = 2048;

@@ -354,6 +354,9 @@ struct mc_model {
     int n_tiles = 0, n_splits = 0, grid = 0;
     bool tiles_ready = false;  // tiles built for the current shape (PBM/UBM build them only for batches)
     std::vector<int64_t> h_tile_begin;  // first session of each tile, ascending (adjoint range lookups)
+    // Launch shapes of the count kernels (entry kernel; dense PBM kernel).
+    CountShape count_shape{8, 256, 8};
+    CountShape dense_shape{0, 256, 6};
     unsigned char* d_tblk = nullptr;
     int64_t split_bins_count = 0;
     int64_t tile_bytes = 0;
@@ -1109,10 +1112,10 @@ extern "C" int mc_model_get_config(const mc_model* m, int32_t* spt, int32_t* wqd
 // One fused iteration: PBM and UBM from their per-(qd, key) counts, the
 // other models (or sizes beyond the count format) through the tile kernel.
 static cudaError_t launch_fused_once(mc_model* m, cudaStream_t st) {
-    if (m->d_cdense) return launch_em_counts_pbm_dense(m->d_fit, m->d_cdense, m->n_qd, m->n_sm, st);
-    if (m->d_coff) return launch_em_counts(m->d_fit, m->d_coff, m->d_cent, m->n_qd, m->n_sm, st);
+    if (m->d_cdense) return launch_em_counts_pbm_dense(m->d_fit, m->d_cdense, m->n_qd, m->n_sm, m->dense_shape, st);
+    if (m->d_coff) return launch_em_counts(m->d_fit, m->d_coff, m->d_cent, m->n_qd, m->n_sm, m->count_shape, st);
     return launch_em_fused(m->model, m->d_fit, m->d_tiles, m->n_tiles, m->d_splits, m->d_ws, m->wqd, m->spt, m->stages,
-                           m->grid, m->block, st);
+                           m->grid, m->block, nullptr, 0, 0, st);
 }
 
 static int launch_fused_loop(mc_model* m, int iters, cudaStream_t st) {
@@ -1379,11 +1382,59 @@ extern "C" int mc_model_em_trace(mc_model* m, int32_t iters, double* train_ll, v
     return MC_OK;
 }
 
+// Times 3 fused iterations (after one warm-up) of the model's current shape.
+static int time_fused(mc_model* m, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1, float* ms) {
+    if (launch_fused_loop(m, 1, st) != MC_OK) return MC_ERR_INVALID;
+    CK(cudaEventRecord(e0, st));
+    if (launch_fused_loop(m, 3, st) != MC_OK) return MC_ERR_INVALID;
+    CK(cudaEventRecord(e1, st));
+    CK(cudaEventSynchronize(e1));
+    CK(cudaEventElapsedTime(ms, e0, e1));
+    return MC_OK;
+}
+
+// Count path: bin copies, block size and blocks per SM of the count kernel.
+static int autotune_counts(mc_model* m, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1) {
+    const bool dense = m->d_cdense != nullptr;
+    const CountShape entry_cands[] = {{8, 256, 8}, {16, 256, 6}, {4, 256, 8}, {8, 128, 16}, {16, 128, 12}, {8, 192, 10}};
+    const CountShape dense_cands[] = {{0, 256, 6}, {0, 256, 8}, {0, 128, 12}, {0, 128, 16}, {0, 192, 8}, {0, 256, 4}};
+    CountShape& shape = dense ? m->dense_shape : m->count_shape;
+    CountShape pick = shape;
+    float best = 1e30f;
+    for (const CountShape& c : dense ? dense_cands : entry_cands) {
+        shape = c;
+        float ms = 0.f;
+        if (time_fused(m, st, e0, e1, &ms) != MC_OK) continue;
+        if (ms < best) { best = ms; pick = c; }
+    }
+    shape = pick;
+    return MC_OK;
+}
+
+extern "C" int mc_model_configure_counts(mc_model* m, int32_t copies, int32_t block, int32_t blocks_per_sm) {
+    if (!m) return set_error(MC_ERR_INVALID, "model_configure_counts: null model");
+    const bool dense = m->d_cdense != nullptr;
+    CountShape c{dense ? 0 : copies, block, blocks_per_sm};
+    if (!count_shape_valid(c, dense))
+        return set_error(MC_ERR_INVALID, "model_configure_counts: copies 4, 8 or 16; block a multiple of 32 in [64, 256]; "
+                                         "blocks per SM in [1, 32]");
+    (dense ? m->dense_shape : m->count_shape) = c;
+    return MC_OK;
+}
+
+extern "C" int mc_model_get_count_config(const mc_model* m, int32_t* copies, int32_t* block, int32_t* blocks_per_sm) {
+    if (!m) return set_error(MC_ERR_INVALID, "model_get_count_config: null model");
+    const CountShape& c = m->d_cdense ? m->dense_shape : m->count_shape;
+    if (copies) *copies = c.copies;
+    if (block) *block = c.block;
+    if (blocks_per_sm) *blocks_per_sm = c.blocks_per_sm;
+    return MC_OK;
+}
+
 extern "C" int mc_model_autotune(mc_model* m, void* stream) {
     if (!m) return set_error(MC_ERR_INVALID, "autotune: null model");
     if (!m->uploaded || (!m->fused_ok && !m->d_coff))
         return set_error(MC_ERR_STATE, "autotune: needs uploaded sessions and the fused path");
-    if (m->d_coff) return MC_OK;  // the count kernel has no tile shape to tune
     CK(cudaSetDevice(m->device));
     cudaStream_t st = m->pick(stream);
     CK(cudaStreamSynchronize(st));
@@ -1394,6 +1445,23 @@ extern "C" int mc_model_autotune(mc_model* m, void* stream) {
     if (m->d_sat) { sat.resize(atr.size()); CK(cudaMemcpy(sat.data(), m->d_sat, sat.size() * 4, cudaMemcpyDeviceToHost)); }
     CK(cudaMemcpy(th.data(), m->d_pub_theta, th.size() * 4, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(&it0, m->d_iter, 4, cudaMemcpyDeviceToHost));
+    auto restore = [&]() -> int {
+        CK(cudaMemcpy(m->d_atr, atr.data(), atr.size() * 4, cudaMemcpyHostToDevice));
+        if (m->d_sat) CK(cudaMemcpy(m->d_sat, sat.data(), sat.size() * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(m->d_pub_theta, th.data(), th.size() * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(m->d_iter, &it0, 4, cudaMemcpyHostToDevice));
+        return check_status(m, st);
+    };
+    if (m->d_coff) {
+        cudaEvent_t c0, c1;
+        CK(cudaEventCreate(&c0));
+        CK(cudaEventCreate(&c1));
+        int rc = autotune_counts(m, st, c0, c1);
+        cudaEventDestroy(c0);
+        cudaEventDestroy(c1);
+        if (rc) return rc;
+        return restore();
+    }
     struct Cand { int spt, wqd, block; };
     const Cand cands[] = {{1024, 1536, 256}, {512, 1024, 256}, {1024, 1024, 256}, {2048, 1536, 256},
                           {512, 1024, 160}, {1024, 1536, 192}, {512, 768, 160}, {256, 512, 128}};
@@ -1405,13 +1473,8 @@ extern "C" int mc_model_autotune(mc_model* m, void* stream) {
     for (const Cand& c : cands) {
         m->spt = c.spt; m->wqd = c.wqd; m->block = c.block;
         if (m->build_tiles() != MC_OK) continue;
-        if (launch_fused_loop(m, 1, st) != MC_OK) continue;  // warm-up
-        CK(cudaEventRecord(e0, st));
-        if (launch_fused_loop(m, 3, st) != MC_OK) continue;
-        CK(cudaEventRecord(e1, st));
-        CK(cudaEventSynchronize(e1));
         float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (time_fused(m, st, e0, e1, &ms) != MC_OK) continue;
         if (ms < best) { best = ms; pick = c; }
     }
     cudaEventDestroy(e0);
@@ -1419,11 +1482,7 @@ extern "C" int mc_model_autotune(mc_model* m, void* stream) {
     m->spt = pick.spt; m->wqd = pick.wqd; m->block = pick.block;
     int rc = m->build_tiles();
     if (rc) return rc;
-    CK(cudaMemcpy(m->d_atr, atr.data(), atr.size() * 4, cudaMemcpyHostToDevice));
-    if (m->d_sat) CK(cudaMemcpy(m->d_sat, sat.data(), sat.size() * 4, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(m->d_pub_theta, th.data(), th.size() * 4, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(m->d_iter, &it0, 4, cudaMemcpyHostToDevice));
-    return check_status(m, st);
+    return restore();
 }
 
 extern "C" int mc_model_fused_path(const mc_model* m, int32_t* path, int64_t* n_entries) {
@@ -1476,6 +1535,11 @@ struct mc_batch {
     // Fits on the count path (PBM/UBM) run in one batched count launch.
     CountFitDev* d_cfits = nullptr;
     int n_cfits = 0, count_blocks = 0;
+    // Count chunks taken by the tile launch itself (one launch per iteration)
+    // or by a count launch after it (the default: measured faster, since the
+    // count kernel runs more warps per SM than the tile kernel's two CTAs).
+    bool single_launch = false;
+    int grid_cap = 1;  // resident tile-kernel CTAs on the device
     mc_model::GraphSlot graphs[2];
     cudaStream_t own_stream = nullptr;
     int64_t bytes = 0;
@@ -1493,10 +1557,17 @@ struct mc_batch {
 // batched count kernel over the count-path fits.
 static int batch_launch_loop(mc_batch* b, int iters, cudaStream_t st) {
     for (int i = 0; i < iters; i++) {
-        if (b->n_tiles)
+        // single_launch: the tile kernel takes the count chunks of the
+        // count-path fits after its tiles; otherwise a count launch follows
+        // the tile launch.  A batch without tile fits runs the count kernel.
+        const bool merged = b->single_launch && b->n_tiles && b->n_cfits;
+        if (b->n_tiles) {
+            const int grid = std::max(1, std::min(b->n_tiles + (merged ? b->count_blocks : 0), b->grid_cap));
             CK(launch_em_fused(b->kernel_model, b->d_fits, b->d_tiles, b->n_tiles, b->d_splits, b->d_ws, b->wqd, b->spt,
-                               b->stages, b->grid, b->block, st));
-        if (b->n_cfits) CK(launch_em_counts_batch(b->d_cfits, b->n_cfits, b->count_blocks, st));
+                               b->stages, grid, b->block, merged ? b->d_cfits : nullptr, merged ? b->n_cfits : 0,
+                               merged ? b->count_blocks : 0, st));
+        }
+        if (b->n_cfits && !merged) CK(launch_em_counts_batch(b->d_cfits, b->n_cfits, b->count_blocks, st));
     }
     return MC_OK;
 }
@@ -1599,7 +1670,7 @@ extern "C" int mc_batch_create(int n_models, mc_model* const* models, mc_batch**
     int best = -1;
     size_t best_smem = 0;
     for (int ns_ = 2; ns_ <= FUSED_MAX_STAGES && e == cudaSuccess; ns_++) {
-        size_t sm_ = fused_smem_bytes(b->kernel_model, b->wqd, b->spt, ns_);
+        size_t sm_ = fused_smem_bytes(b->kernel_model, b->wqd, b->spt, ns_, b->n_cfits > 0);
         if (sm_ + 4096 > (size_t)optin) break;
         if ((e = fused_set_smem_limits(sm_)) != cudaSuccess) break;
         int per_sm = 0;
@@ -1614,7 +1685,7 @@ extern "C" int mc_batch_create(int n_models, mc_model* const* models, mc_batch**
         delete b;
         return e != cudaSuccess ? cuda_fail("batch_create", e) : set_error(MC_ERR_INVALID, "batch_create: tile shape does not fit");
     }
-    b->grid = std::max(1, std::min(b->n_tiles, b->grid * b->n_sm));
+    b->grid_cap = b->grid * b->n_sm;
     *out = b;
     return MC_OK;
 }
@@ -1660,6 +1731,25 @@ extern "C" int mc_batch_info(const mc_batch* b, int32_t* n_models, int32_t* n_ti
     if (n_models) *n_models = (int32_t)b->models.size();
     if (n_tiles) *n_tiles = b->n_tiles;
     if (mixed_models) *mixed_models = b->kernel_model < 0;
+    return MC_OK;
+}
+
+extern "C" int mc_batch_configure(mc_batch* b, int single_launch) {
+    if (!b) return set_error(MC_ERR_INVALID, "batch_configure: null batch");
+    if (b->single_launch != (single_launch != 0)) {
+        b->single_launch = single_launch != 0;
+        for (auto& g : b->graphs) {  // recaptured on the next mc_batch_em
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+            g.iters = -1;
+        }
+    }
+    return MC_OK;
+}
+
+extern "C" int mc_batch_launches(const mc_batch* b, int32_t* launches_per_iteration) {
+    if (!b || !launches_per_iteration) return set_error(MC_ERR_INVALID, "batch_launches: null argument");
+    *launches_per_iteration = (b->n_tiles ? 1 : 0) + (b->n_cfits && !(b->single_launch && b->n_tiles) ? 1 : 0);
     return MC_OK;
 }
 

@@ -102,6 +102,7 @@ def test_count_path_fits_batch_without_tiles():
     b = api.Batch(models)
     n_models, n_tiles, mixed = b.info()
     assert (n_models, n_tiles, mixed) == (len(parts), 0, 0)
+    assert b.launches_per_iteration() == 1
     b.em(6)
     for (model, train, n_qd), cm in zip(parts, models):
         f = bindings.OracleFit("f64", model, 0, train.query, train.pidx, train.click, n_qd)
@@ -110,8 +111,11 @@ def test_count_path_fits_batch_without_tiles():
     b.close()
 
 
-def test_batch_of_both_paths_runs_the_specialised_tile_kernel():
-    """DBN tile fits next to PBM/UBM count fits: the tile launch holds DBN only."""
+@pytest.mark.parametrize("single_launch", [False, True])
+def test_batch_of_both_paths_runs_the_specialised_tile_kernel(single_launch):
+    """DBN tile fits next to PBM/UBM count fits: the tile launch holds DBN
+    only; its count chunks go to a count launch after it, or (single_launch)
+    to the tile launch itself after its tiles."""
     parts = []
     for name, model in [("dbn_dbnclicks", 2), ("pbm_pbmclicks", 0), ("ubm_dbnclicks", 3), ("edge", 2)]:
         c = load_case(name)
@@ -120,6 +124,9 @@ def test_batch_of_both_paths_runs_the_specialised_tile_kernel():
     b = api.Batch(models)
     n_models, n_tiles, mixed = b.info()
     assert n_models == len(parts) and n_tiles > 0 and not mixed
+    assert b.launches_per_iteration() == 2
+    b.configure(single_launch)
+    assert b.launches_per_iteration() == (1 if single_launch else 2)
     b.em(5)
     for (model, train, n_qd), cm in zip(parts, models):
         f = bindings.OracleFit("f64", model, 0, train.query, train.pidx, train.click, n_qd)

@@ -139,3 +139,44 @@ def test_pbm_count_above_16_bits_takes_the_entry_path():
     f = bindings.OracleFit("f64", api.PBM, 0, ds.train.query, ds.train.pidx, ds.train.click, ds.n_qd)
     f.run(4)
     _close(cm.get_parameters(), f.values(), "pbm 16-bit overflow")
+
+
+@pytest.mark.parametrize("model,shapes", [
+    (api.UBM, [(4, 256, 8), (8, 128, 16), (16, 192, 10), (16, 64, 32)]),
+    (api.PBM, [(0, 128, 12), (0, 64, 32), (0, 256, 4)]),
+])
+def test_count_shapes_do_not_change_results(model, shapes):
+    """The count kernels' launch shape (bin copies, block, blocks per SM) is a
+    tuning knob only; the autotuner picks one of its candidates and leaves
+    the parameters where they were."""
+    case = load_case("ubm_dbnclicks" if model == api.UBM else "pbm_pbmclicks")
+    f = bindings.OracleFit("f64", model, 0, case["train_query"], case["train_pidx"], case["train_click"],
+                           int(case["n_qd"]))
+    f.run(5)
+    for shape in shapes:
+        cm = api.ClickModel.create(model)
+        cm.upload(_sset(case), int(case["n_qd"]))
+        cm.configure_counts(*shape)
+        got = cm.count_config()
+        assert got[1:] == shape[1:] and (model == api.PBM or got[0] == shape[0])
+        cm.em(5)
+        _close(cm.get_parameters(), f.values(), f"m{model} shape {shape}")
+    cm = api.ClickModel.create(model)
+    cm.upload(_sset(case), int(case["n_qd"]))
+    cm.em(2)
+    before = cm.get_parameters()
+    cm.autotune()
+    after = cm.get_parameters()
+    for k in before:
+        assert np.array_equal(before[k], after[k])
+    cm.em(3)
+    _close(cm.get_parameters(), f.values(), f"m{model} autotuned {cm.count_config()}")
+
+
+def test_count_shape_rejects_bad_values():
+    case = load_case("ubm_dbnclicks")
+    cm = api.ClickModel.create(api.UBM)
+    cm.upload(_sset(case), int(case["n_qd"]))
+    for bad in [(3, 256, 8), (8, 96 + 1, 8), (8, 512, 8), (8, 256, 0), (8, 32, 8)]:
+        with pytest.raises(api._capi.MCError):
+            cm.configure_counts(*bad)
