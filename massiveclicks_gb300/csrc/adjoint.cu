@@ -14,6 +14,9 @@
 // through the model's tiles, with the gradient summed per tile in shared
 // memory; other session orders through FP64 global atomics per session.
 #include <cstdint>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -28,6 +31,11 @@ __device__ __forceinline__ T sigm(float x) {
 
 template <typename T>
 __device__ __forceinline__ T tlog(T x) { return log(x); }
+
+// 1 / x, correctly rounded in both precisions (the FP32 reciprocal
+// instruction with round-to-nearest costs a fraction of a full division).
+__device__ __forceinline__ float rcp(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
 
 __device__ __forceinline__ double warp_sum_dd(double v) {
 #pragma unroll
@@ -129,8 +137,10 @@ __host__ __device__ constexpr int adjoint_smem_elems(int window_max) {
                                                                         : 2 * kSmallWin + 2 * kSmallWin * kSmallCopies;
 }
 
+// Three 256-thread blocks per SM in FP32 (at most 85 registers; a few spill),
+// which measured faster than two without spills; FP64 is the checking path.
 template <typename T>
-__global__ void __launch_bounds__(256) adjoint_tiles_kernel(AdjointArgs A, const TileDev* __restrict__ tiles, int t0,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) adjoint_tiles_kernel(AdjointArgs A, const TileDev* __restrict__ tiles, int t0,
                                                            int t1, int window_max, bool grad) {
     extern __shared__ __align__(16) unsigned char sm[];
     // Wide window: va, vs, ga, gb of window_max entries each.  Small window
@@ -167,13 +177,30 @@ __global__ void __launch_bounds__(256) adjoint_tiles_kernel(AdjointArgs A, const
                 for (int i = threadIdx.x; i < 2 * kSmallWin * kSmallCopies; i += blockDim.x) cp[i] = T(0);
             __syncthreads();
         }
+        // Each thread loads its next session's indices and clicks while it
+        // works on the current one (global loads are the longest wait here).
+        int pn[MC_R];
+        unsigned mn = 0;
+        if (s0 + threadIdx.x < s1) {
+            mn = A.click[s0 + threadIdx.x];
+#pragma unroll
+            for (int r = 0; r < MC_R; r++) pn[r] = A.pidx[(int64_t)r * A.stride + s0 + threadIdx.x];
+        }
         for (int64_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
             int rl[MC_R];
-            T a[MC_R], sv[MC_R], ex[MC_R + 1], pr[MC_R];
-            const unsigned m = A.click[s];
+            T a[MC_R], sv[MC_R], ex[MC_R + 1], ip[MC_R];  // ip: 1 / p of unclicked ranks
+            const unsigned m = mn;
+            int pc[MC_R];
+#pragma unroll
+            for (int r = 0; r < MC_R; r++) pc[r] = pn[r];
+            if (s + blockDim.x < s1) {
+                mn = A.click[s + blockDim.x];
+#pragma unroll
+                for (int r = 0; r < MC_R; r++) pn[r] = A.pidx[(int64_t)r * A.stride + s + blockDim.x];
+            }
 #pragma unroll
             for (int r = 0; r < MC_R; r++) {
-                const int p = A.pidx[(int64_t)r * A.stride + s];
+                const int p = pc[r];
                 // A tile's sessions show only its window's pairs (the tiles
                 // are built so); the clamp keeps shared-memory accesses in
                 // bounds regardless.
@@ -185,14 +212,17 @@ __global__ void __launch_bounds__(256) adjoint_tiles_kernel(AdjointArgs A, const
             T lls = T(0);
 #pragma unroll
             for (int r = 0; r < MC_R; r++) {
+                T pr;
                 if ((m >> r) & 1u) {
-                    pr[r] = a[r] * ex[r];
+                    pr = a[r] * ex[r];
                     ex[r + 1] = g * (T(1) - sv[r]);
+                    ip[r] = T(0);
                 } else {
-                    pr[r] = T(1) - a[r] * ex[r];
-                    ex[r + 1] = ex[r] * g * (T(1) - a[r]) / pr[r];
+                    pr = T(1) - a[r] * ex[r];
+                    ip[r] = rcp(pr);
+                    ex[r + 1] = ex[r] * g * (T(1) - a[r]) * ip[r];
                 }
-                lls += tlog(pr[r]);
+                lls += tlog(pr);
             }
             ll += (double)lls;
             if (!grad) continue;
@@ -201,18 +231,18 @@ __global__ void __launch_bounds__(256) adjoint_tiles_kernel(AdjointArgs A, const
             for (int r = MC_R - 1; r >= 0; r--) {
                 T a_bar, ex_bar;
                 if ((m >> r) & 1u) {
-                    a_bar = T(1) / a[r];
-                    ex_bar = T(1) / ex[r];
+                    a_bar = rcp(a[r]);
+                    ex_bar = rcp(ex[r]);
                     g_bar_acc += e_bar * (T(1) - sv[r]);
                     const T db = w * (-e_bar * g) * sv[r] * (T(1) - sv[r]);
                     if (small) atomicAdd(my + kSmallWin + rl[r], db);
                     else if (staged) atomicAdd(gb + rl[r], db);
                     else atomicAdd(A.g_beta + rl[r], (double)db);
                 } else {
-                    const T ip = T(1) / pr[r];
-                    a_bar = -ex[r] * ip + e_bar * ex[r] * g * (ex[r] - T(1)) * ip * ip;
-                    ex_bar = -a[r] * ip + e_bar * g * (T(1) - a[r]) * ip * ip;
-                    g_bar_acc += e_bar * ex[r] * (T(1) - a[r]) * ip;
+                    const T q = ip[r];
+                    a_bar = -ex[r] * q + e_bar * ex[r] * g * (ex[r] - T(1)) * q * q;
+                    ex_bar = -a[r] * q + e_bar * g * (T(1) - a[r]) * q * q;
+                    g_bar_acc += e_bar * ex[r] * (T(1) - a[r]) * q;
                 }
                 const T da = w * a_bar * a[r] * (T(1) - a[r]);
                 if (small) atomicAdd(my + rl[r], da);
@@ -282,16 +312,41 @@ size_t adjoint_tiles_smem(int window_max, bool fp64) {
     return (size_t)adjoint_smem_elems<float>(window_max) * (fp64 ? 8 : 4);
 }
 
+// Resident blocks per SM of the tile kernel for a shared-memory size, per
+// device and precision, found once: the attribute and occupancy queries cost
+// more host time than a minibatch's kernel.  The kernel's dynamic
+// shared-memory limit only ever grows, so no call shrinks it under another.
+static int adjoint_blocks_per_sm(bool fp64, size_t smem, cudaError_t* err) {
+    static std::mutex mu;
+    static std::map<std::tuple<int, bool, size_t>, int> cache;
+    static std::map<std::pair<int, bool>, size_t> limit;
+    int dev = 0;
+    *err = cudaGetDevice(&dev);
+    if (*err != cudaSuccess) return 0;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find({dev, fp64, smem});
+    if (it != cache.end()) return it->second;
+    size_t& lim = limit[{dev, fp64}];
+    if (smem > lim) {
+        *err = fp64 ? cudaFuncSetAttribute(adjoint_tiles_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                    : cudaFuncSetAttribute(adjoint_tiles_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (*err != cudaSuccess) return 0;
+        lim = smem;
+    }
+    int per_sm = 0;
+    *err = fp64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_tiles_kernel<double>, 256, smem)
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_tiles_kernel<float>, 256, smem);
+    if (*err != cudaSuccess) return 0;
+    cache[{dev, fp64, smem}] = per_sm;
+    return per_sm;
+}
+
 cudaError_t launch_adjoint_tiles(const AdjointArgs& A, const TileDev* tiles, int t0, int t1, int window_max, bool grad,
                                  bool fp64, int n_sm, cudaStream_t st) {
     if (A.count <= 0 || t1 <= t0) return cudaSuccess;
     const size_t smem = adjoint_tiles_smem(window_max, fp64);
-    cudaError_t e = fp64 ? cudaFuncSetAttribute(adjoint_tiles_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                         : cudaFuncSetAttribute(adjoint_tiles_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = fp64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_tiles_kernel<double>, 256, smem)
-             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_tiles_kernel<float>, 256, smem);
+    cudaError_t e = cudaSuccess;
+    const int per_sm = adjoint_blocks_per_sm(fp64, smem, &e);
     if (e != cudaSuccess) return e;
     const int n = t1 - t0;
     const int cap = (per_sm > 0 ? per_sm : 1) * n_sm;
