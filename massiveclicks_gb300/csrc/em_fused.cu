@@ -1081,10 +1081,11 @@ cudaError_t fused_occupancy(int model, int block, size_t smem, int* blocks_per_s
 // Packs the tiles' sessions into the staged layout: per tile, rank-major
 // uint16 window-relative indices [10][spad] followed by the click masks
 // [spad] (padding zeroed), spad = s_packed rounded up to 8.  Sessions are
-// ordered by click pattern (DBN/CCM: last-click rank, then mask; PBM/UBM:
-// click mask) so the lanes of a warp take the same branches: a block radix
-// sort of (pattern << 16 | position) on the 14 pattern bits, stable, so equal
-// patterns keep their session order.  DBN and CCM sessions without clicks
+// ordered by click pattern (DBN: last-click rank; CCM: last-click rank, then
+// mask; PBM/UBM: click mask) so the lanes of a warp take the same branches: a
+// block radix sort of (pattern << 16 | position) on the pattern bits the
+// model's E-step branches on, stable, so equal patterns keep their session
+// order.  DBN and CCM sessions without clicks
 // carry no variable statistic (their constant contributions are folded in at
 // upload) and are left out; s_packed records how many sessions remain.
 // Direct tiles keep no packed block.
@@ -1105,7 +1106,7 @@ union PackSortStorage {
 // positions past the tile get the largest key.  Sorted keys go to keys[].
 template <int ITEMS>
 __device__ __forceinline__ void pack_sort(PackSortStorage& tmp, uint32_t* keys, const uint16_t* click, int64_t s_begin,
-                                          int s_count, bool drop_clickless) {
+                                          int s_count, bool drop_clickless, int begin_bit) {
     uint32_t k[ITEMS];
 #pragma unroll
     for (int j = 0; j < ITEMS; j++) {
@@ -1120,7 +1121,7 @@ __device__ __forceinline__ void pack_sort(PackSortStorage& tmp, uint32_t* keys, 
     }
     // Patterns are below 0x2800; clickless sessions and padding (0xFFFF) read
     // 0x3FFF on bits [16, 30) and sort after them, padding last (stability).
-    PackSort<ITEMS>(reinterpret_cast<typename PackSort<ITEMS>::TempStorage&>(tmp)).Sort(k, 16, 30);
+    PackSort<ITEMS>(reinterpret_cast<typename PackSort<ITEMS>::TempStorage&>(tmp)).Sort(k, begin_bit, 30);
 #pragma unroll
     for (int j = 0; j < ITEMS; j++) keys[threadIdx.x * ITEMS + j] = k[j];
 }
@@ -1137,12 +1138,16 @@ __global__ void __launch_bounds__(kPackThreads) pack_tiles_kernel(int model, Til
         if (tile.qd_count > window_max) continue;
         for (int i = threadIdx.x; i < tile.qd_count; i += blockDim.x) occ[i] = 0;
         const bool drop_clickless = model == DBN || model == CCM;
+        // The DBN E-step branches on the last-click rank only: one radix pass
+        // over its 4 bits; CCM also on the clicks before it, PBM / UBM on the
+        // mask: the 14 pattern bits.
+        const int begin_bit = model == DBN ? 26 : 16;
         if (tile.s_count <= 4 * kPackThreads)
-            pack_sort<4>(sort_tmp, keys, click, tile.s_begin, tile.s_count, drop_clickless);
+            pack_sort<4>(sort_tmp, keys, click, tile.s_begin, tile.s_count, drop_clickless, begin_bit);
         else if (tile.s_count <= 8 * kPackThreads)
-            pack_sort<8>(sort_tmp, keys, click, tile.s_begin, tile.s_count, drop_clickless);
+            pack_sort<8>(sort_tmp, keys, click, tile.s_begin, tile.s_count, drop_clickless, begin_bit);
         else
-            pack_sort<16>(sort_tmp, keys, click, tile.s_begin, tile.s_count, drop_clickless);
+            pack_sort<16>(sort_tmp, keys, click, tile.s_begin, tile.s_count, drop_clickless, begin_bit);
         __syncthreads();
         int kept = 0;
         for (int i = threadIdx.x; i < tile.s_count; i += blockDim.x) kept += (keys[i] >> 16) != 0xFFFFu;
