@@ -214,13 +214,46 @@ struct GlobSrc {
 // here, and at about nine adds per session they were a third of the launch.
 // The fixed-point sum of a bin is exact (integer addition, any order); each
 // added value carries one rounding of at most 2^-(shift+1).
+//
+// Attractiveness values are proportional to the pair's own attractiveness a,
+// which ranges over several decades (2e-4 for a pair that is rarely clicked),
+// so one absolute step per tile would cost a small-a pair most of its
+// relative precision.  Each attractiveness add is therefore scaled by a
+// further 2^b(a), with b(a) = 126 - (biased exponent of a) clamped to
+// [0, kMaxBoost]: a 2^b(a) lies in [1/2, 1), and every add of one pair in one
+// tile sees the same a (the values of the iteration before), so the bin is
+// one fixed-point sum with step 2^-(shift + b).  The pair's b is stored in
+// the tile's boost slot (the same byte from every add) for the M-step, which
+// takes 2^-(shift + b) in place of 2^-shift.
+constexpr int kMaxBoost = 60;
+
+__device__ __forceinline__ int value_boost(float a) {
+    const int b = 126 - ((__float_as_int(a) >> 23) & 0xFF);
+    return b < 0 ? 0 : (b > kMaxBoost ? kMaxBoost : b);
+}
+
+// 2^-b times a power of two x (b <= kMaxBoost, x >= 2^-31): exponent arithmetic, exact.
+__device__ __forceinline__ float unboost(float x, int b) { return __int_as_float(__float_as_int(x) - (b << 23)); }
+
 struct SmemSink {
     float* bins;
     int stride;
-    float scale;  // 2^shift for fixed point, 0 for FP32
+    float scale;     // 2^shift for fixed point, 0 for FP32
+    uint8_t* boost;  // b(a) of each window entry of this tile (fixed point)
     __device__ __forceinline__ void add(int rl, int k, float v) const {
         if (scale != 0.0f) atomicAdd(reinterpret_cast<unsigned*>(bins) + k * stride + rl, __float2uint_rn(v * scale));
         else atomicAdd(bins + k * stride + rl, v);
+    }
+    // Attractiveness statistic (k = 0) of an entry whose attractiveness is a.
+    __device__ __forceinline__ void add_a(int rl, float v, float a) const {
+        if (scale != 0.0f) {
+            const int b = value_boost(a);
+            boost[rl] = (uint8_t)b;
+            const float sc = __int_as_float(__float_as_int(scale) + (b << 23));
+            atomicAdd(reinterpret_cast<unsigned*>(bins) + rl, __float2uint_rn(v * sc));
+        } else {
+            atomicAdd(bins + rl, v);
+        }
     }
 };
 
@@ -228,6 +261,8 @@ struct SmemSink {
 // per packed (session, rank) showing its pair, so at most max_occ values (the
 // tile's largest packed occurrence count, found when the tile is packed),
 // each below 2^ev (fx_value_exponent).  shift = 31 - ceil(log2 max_occ) - ev.
+// A boosted attractiveness value is v 2^b(a) = (v / a)(a 2^b(a)) < v / a, and
+// fx_value_exponent bounds v / a as well as v.
 constexpr int FX_MIN_SHIFT = 20;
 
 __device__ __forceinline__ float fx_scale(int max_occ, int ev) {
@@ -240,8 +275,10 @@ __device__ __forceinline__ float fx_scale(int max_occ, int ev) {
 // ev with every private statistic value below 2^ev, with a factor 2 of margin
 // for rounding.  DBN attractiveness a(1 - eps)/(1 - eps car) and satisfaction
 // s/(1 - (1 - s) g car), the CCM unclicked attractiveness term and the PBM /
-// UBM terms are at most 1 (car <= 1, eps <= 1).  The CCM term of a clicked
-// last rank, a / (1 - (t2 (1 - a) + t3 a) car), is at most 1 / (1 - max(t2, t3)).
+// UBM terms (a - ae)/(1 - ae) are at most 1 (car <= 1, eps <= 1, e <= 1), and
+// so are their attractiveness terms divided by a.  The CCM term of a clicked
+// last rank, a / (1 - (t2 (1 - a) + t3 a) car), and that term divided by a,
+// are at most 1 / (1 - max(t2, t3)).
 __device__ __forceinline__ int fx_value_exponent(int model, const float* pub) {
     if (model != CCM) return 1;
     const float tm = fmaxf(pub[1], pub[2]);
@@ -253,6 +290,7 @@ struct GlobSink {
     double* bins;
     int ns;
     __device__ __forceinline__ void add(int rl, int k, float v) const { atomicAdd(bins + (int64_t)rl * ns + k, (double)v); }
+    __device__ __forceinline__ void add_a(int rl, float v, float) const { add(rl, 0, v); }
 };
 
 // ---------------------------------------------------------------------------
@@ -271,7 +309,7 @@ __device__ __forceinline__ void estep_pbm(const Src& src, const Sink& sink, int 
             float e = pub[r];
             float ae = a * e;
             float inv = __fdividef(1.0f, 1.0f - ae);
-            sink.add(rl[r], 0, (a - ae) * inv);
+            sink.add_a(rl[r], (a - ae) * inv, a);
             acc[r] += (e - ae) * inv;
         }
     }
@@ -308,7 +346,7 @@ __device__ __forceinline__ void estep_ubm(const Src& src, const Sink& sink, int 
             float e = pub[slot[r]];
             float ae = a * e;
             float inv = __fdividef(1.0f, 1.0f - ae);
-            sink.add(rl[r], 0, (a - ae) * inv);
+            sink.add_a(rl[r], (a - ae) * inv, a);
             if (alive) { key[r] = slot[r]; var[r] = (e - ae) * inv; }
         }
     }
@@ -423,7 +461,7 @@ __device__ __forceinline__ void estep_dbn(const Src& src, const Sink& sink, int 
             const float D = __fdividef(1.0f, P - u);
             gnum += t * R * D;
             gden += (E - u) * D;
-            sink.add(rl, 0, __fdividef(a[r] * (1.0f - eps), 1.0f - eps * car[r]));
+            sink.add_a(rl, __fdividef(a[r] * (1.0f - eps), 1.0f - eps * car[r]), a[r]);
             P = P - a[r] * E;
             E = t * (1.0f - a[r]);
             rescale(P, E);
@@ -490,7 +528,7 @@ __device__ __forceinline__ void estep_ccm(const Src& src, const Sink& sink, int 
             t[2] += ia * t2 * R * B; t[3] += ia * k2 * B;
             t[4] += a[r] * t3 * R * B; t[5] += a[r] * k3 * B;
             float cont = t2 * ia + t3 * a[r];
-            sink.add(rls[r], 0, __fdividef(a[r], 1.0f - cont * car[r + 1]));
+            sink.add_a(rls[r], __fdividef(a[r], 1.0f - cont * car[r + 1]), a[r]);
             E = cont;
             P = 1.0f;
         } else {
@@ -500,7 +538,7 @@ __device__ __forceinline__ void estep_ccm(const Src& src, const Sink& sink, int 
             const float D = __fdividef(1.0f, P - u);
             t[0] += te * R * D;
             t[1] += (E - u) * D;
-            sink.add(rls[r], 0, __fdividef((1.0f - eps) * a[r], 1.0f - eps * car[r]));
+            sink.add_a(rls[r], __fdividef((1.0f - eps) * a[r], 1.0f - eps * car[r]), a[r]);
             P = P - a[r] * E;
             E = te * ia;
             rescale(P, E);
@@ -571,11 +609,15 @@ __device__ void finalize_public(const FitDev& f, int ctid, int nc, int* s_it) {
 //            is a private statistic, else 1)
 //   counts   uint32 [2 slots][window_max + 8]: the window's 16-bit click-count
 //            pairs of the k-th tile in slot k & 1, read by its M-step
+//   boost    uint8 [2 slots][window_max + 8]: b(a) of the k-th tile's window
+//            entries (fixed-point attractiveness bins) in slot k & 1
 //   stage s  { uint16 rel[10][spt_pad], uint16 clk[spt_pad],
 //              float atr[window_max + 8], float sat[window_max + 8] (DBN) }
 //            for s < n_stages
+// A slot index k & 1 is an element offset of (window_max + 8) in both the
+// count and the boost slots.
 struct Layout {
-    uint32_t bins_stride, bins_buf, cnt_off, cnt_slot, stage_off, stage_bytes, sess_bytes, atr_off, sat_off;
+    uint32_t bins_stride, bins_buf, cnt_off, cnt_slot, boost_off, stage_off, stage_bytes, sess_bytes, atr_off, sat_off;
 };
 
 __host__ __device__ inline int layout_stats(int model) { return (model == DBN || model < 0) ? 2 : 1; }
@@ -589,7 +631,8 @@ __host__ __device__ inline Layout make_layout(int model, int spt, int window_max
     L.bins_buf = nb * (uint32_t)window_max;
     L.cnt_off = (2u * L.bins_buf * 4u + 15u) & ~15u;
     L.cnt_slot = w;
-    L.stage_off = L.cnt_off + ((2u * w * 4u + 15u) & ~15u);
+    L.boost_off = L.cnt_off + ((2u * w * 4u + 15u) & ~15u);
+    L.stage_off = L.boost_off + ((2u * w + 15u) & ~15u);
     L.sess_bytes = 11u * spad * 2u;
     L.atr_off = (L.sess_bytes + 15u) & ~15u;
     L.sat_off = L.atr_off + w * 4u;
@@ -635,6 +678,9 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
     }
     for (int k = tid; k < MC_MAX_PUB; k += blockDim.x) { pub_acc[k] = 0.0; pub_tile[0][k] = 0.0f; pub_tile[1][k] = 0.0f; }
     for (int k = tid; k < (int)(2 * L.bins_buf); k += blockDim.x) bins[k] = 0.0f;
+    // Boost bytes start at 0: an entry without attractiveness adds keeps a
+    // byte <= kMaxBoost, so its M-step factor stays finite (its bin is 0).
+    for (int k = tid; k < (int)(2 * L.cnt_slot); k += blockDim.x) smem[L.boost_off + k] = 0;
     fence_async_shared();
     __syncthreads();
 
@@ -818,6 +864,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             // 2^-shift of the previous tile's bins (exact), 0 for FP32 bins.
             const float inv_prev = sc_prev != 0.0f ? __frcp_rn(sc_prev) : 0.0f;
             const unsigned* ubins_m = reinterpret_cast<const unsigned*>(bins) + ((k - 1) & 1) * L.bins_buf;
+            const uint8_t* boost_m = smem + L.boost_off + ((k - 1) & 1) * L.cnt_slot;
             const int n_sess = t < 0 ? 0 : (direct ? tile.s_count : tile.s_packed);
             const int nE = (n_sess + 31) >> 5;
             const int nM = prev_t < 0 ? 0 : (ptile.split >= 0 ? 1 : (ptile.qd_count + 32 * kMQ - 1) / (32 * kMQ));
@@ -852,7 +899,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
                         if (i < ptile.qd_count) {
                             float v0, v1 = 0.0f;
                             if (inv_prev != 0.0f) {
-                                v0 = __uint2float_rn(ubins_m[i]) * inv_prev;
+                                v0 = __uint2float_rn(ubins_m[i]) * unboost(inv_prev, boost_m[i]);
                                 if (pns > 1) v1 = __uint2float_rn(ubins_m[L.bins_stride + i]) * inv_prev;
                             } else {
                                 v0 = bins_m[i];
@@ -873,7 +920,8 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
                     for (int i = lane; i < ptile.qd_count; i += 32)
                         for (int kk = 0; kk < pns; kk++) {
                             const int j = kk * L.bins_stride + i;
-                            const double v = inv_prev != 0.0f ? (double)ubins_m[j] * (double)inv_prev : (double)bins_m[j];
+                            const float inv = kk == 0 ? unboost(inv_prev, boost_m[i]) : inv_prev;
+                            const double v = inv_prev != 0.0f ? (double)ubins_m[j] * (double)inv : (double)bins_m[j];
                             if (v != 0.0) { atomicAdd(gb + (int64_t)i * pns + kk, v); bins_m[j] = 0.0f; }
                         }
                 }
@@ -912,7 +960,7 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
             gsrc.pidx = f.pidx; gsrc.clk = f.click; gsrc.atr = f.atr; gsrc.sat = f.sat;
             gsrc.stride = f.stride; gsrc.s_begin = tile.s_begin; gsrc.qd_begin = tile.qd_begin;
             gsrc.qd_count = tile.qd_count; gsrc.status = f.status;
-            SmemSink ssink{bins_e, (int)L.bins_stride, sc};
+            SmemSink ssink{bins_e, (int)L.bins_stride, sc, smem + L.boost_off + (k & 1) * L.cnt_slot};
             GlobSink gsink{direct ? f.split_bins + splits[tile.split].bin_offset : nullptr,
                            t >= 0 ? private_stats(model) : 1};
 

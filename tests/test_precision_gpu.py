@@ -3,13 +3,15 @@
 tau = 0.6 / 0.3 / 0.2 and relevance ~ Beta(1, 3)).  DBN and CCM are fitted for
 50 iterations from the prior by
 
-  * fused: FP32 E-step with per-rank scaling, FP32 shared-memory bins per
-    tile, FP64 fold for split queries and public statistics;
+  * fused: FP32 E-step with per-rank scaling, 32-bit fixed-point
+    shared-memory bins per tile (attractiveness values scaled by their
+    parameter's binary exponent), FP64 fold for split queries and public
+    statistics;
   * plain: FP32 E-step in log space, FP32 global atomics (all-FP32);
   * the FP64 oracle: the reference's CPU path in double precision;
 
-and each GPU variant's parameter max-abs error and test log-likelihood and
-perplexity errors against the oracle are printed (one JSON line per model,
+and each GPU variant's parameter max-abs and max-relative errors and test
+log-likelihood and perplexity errors against the oracle are printed (one JSON line per model,
 prefixed PRECISION) and, if MC_PRECISION_OUT names a file, appended to it.
 
 Default size 2M sessions over 100k queries; MC_PRECISION_SESSIONS=20000000
@@ -30,6 +32,7 @@ pytestmark = pytest.mark.gpu
 
 ITERATIONS = 50
 TEST_LL_RTOL = 1e-5
+PARAM_RTOL = 1e-5   # every fused parameter, relative, no absolute term
 
 
 def _errors(got: dict, ref: dict) -> dict:
@@ -87,3 +90,5 @@ def test_precision_against_fp64_oracle(dataset, model):
     # reported, not held to it.
     assert line["fused"]["test_llh_rel_err"] <= TEST_LL_RTOL
     assert line["fused"]["perplexity_rel_err"] <= TEST_LL_RTOL
+    for k, e in line["fused"]["params"].items():
+        assert e["max_rel"] <= PARAM_RTOL, (line["model"], k, e)
