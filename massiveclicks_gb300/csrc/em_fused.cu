@@ -219,27 +219,32 @@ struct GlobSrc {
 // which ranges over several decades (2e-4 for a pair that is rarely clicked),
 // so one absolute step per tile would cost a small-a pair most of its
 // relative precision.  Each attractiveness add is therefore scaled by a
-// further 2^b(a), with b(a) = 126 - (biased exponent of a) clamped to
-// [0, kMaxBoost]: a 2^b(a) lies in [1/2, 1), and every add of one pair in one
-// tile sees the same a (the values of the iteration before), so the bin is
-// one fixed-point sum with step 2^-(shift + b).  The pair's b is stored in
-// the tile's boost slot (the same byte from every add) for the M-step, which
-// takes 2^-(shift + b) in place of 2^-shift.
+// further 2^b, b = 126 - e(a), where e(a) is the biased exponent of a clamped
+// below at 126 - kMaxBoost: for a < 1, a 2^b lies in [1/2, 1) (or below 1/2
+// when clamped).  Every add of one pair in one tile sees the same a (the
+// values of the iteration before), so the bin is one fixed-point sum with
+// step 2^-(shift + b).  Each add stores the pair's e(a) in the tile's boost
+// slot (the same byte from every add); the M-step takes 2^-(shift + b) in
+// place of 2^-shift.  Boost bytes start at 126 (b = 0).  With e in [66, 255]
+// and shift in [FX_MIN_SHIFT, 30], the scale's biased exponent
+// 127 + shift + 126 - e lies in [18, 217] and the M-step factor's
+// 127 - shift + e - 126 in [37, 236]: both normal, built by exponent
+// arithmetic, exact.
 constexpr int kMaxBoost = 60;
 
-__device__ __forceinline__ int value_boost(float a) {
-    const int b = 126 - ((__float_as_int(a) >> 23) & 0xFF);
-    return b < 0 ? 0 : (b > kMaxBoost ? kMaxBoost : b);
+// e(a) << 23: the exponent field of a, at least (126 - kMaxBoost) << 23.
+__device__ __forceinline__ int boost_exponent_bits(float a) {
+    return max(__float_as_int(a) & 0x7F800000, (126 - kMaxBoost) << 23);
 }
 
-// 2^-b times a power of two x (b <= kMaxBoost, x >= 2^-31): exponent arithmetic, exact.
-__device__ __forceinline__ float unboost(float x, int b) { return __int_as_float(__float_as_int(x) - (b << 23)); }
+// 2^-(shift + b) from x = 2^-shift and a stored e(a) byte.
+__device__ __forceinline__ float unboost(float x, int e) { return __int_as_float(__float_as_int(x) + ((e - 126) << 23)); }
 
 struct SmemSink {
     float* bins;
     int stride;
     float scale;     // 2^shift for fixed point, 0 for FP32
-    uint8_t* boost;  // b(a) of each window entry of this tile (fixed point)
+    uint8_t* boost;  // e(a) of each window entry of this tile (fixed point)
     __device__ __forceinline__ void add(int rl, int k, float v) const {
         if (scale != 0.0f) atomicAdd(reinterpret_cast<unsigned*>(bins) + k * stride + rl, __float2uint_rn(v * scale));
         else atomicAdd(bins + k * stride + rl, v);
@@ -247,9 +252,9 @@ struct SmemSink {
     // Attractiveness statistic (k = 0) of an entry whose attractiveness is a.
     __device__ __forceinline__ void add_a(int rl, float v, float a) const {
         if (scale != 0.0f) {
-            const int b = value_boost(a);
-            boost[rl] = (uint8_t)b;
-            const float sc = __int_as_float(__float_as_int(scale) + (b << 23));
+            const int e = boost_exponent_bits(a);
+            boost[rl] = (uint8_t)(e >> 23);
+            const float sc = __int_as_float(__float_as_int(scale) + (126 << 23) - e);
             atomicAdd(reinterpret_cast<unsigned*>(bins) + rl, __float2uint_rn(v * sc));
         } else {
             atomicAdd(bins + rl, v);
@@ -261,8 +266,8 @@ struct SmemSink {
 // per packed (session, rank) showing its pair, so at most max_occ values (the
 // tile's largest packed occurrence count, found when the tile is packed),
 // each below 2^ev (fx_value_exponent).  shift = 31 - ceil(log2 max_occ) - ev.
-// A boosted attractiveness value is v 2^b(a) = (v / a)(a 2^b(a)) < v / a, and
-// fx_value_exponent bounds v / a as well as v.
+// A boosted attractiveness value is v 2^b = (v / a)(a 2^b) < v / a for a < 1,
+// and fx_value_exponent bounds v / a as well as v.
 constexpr int FX_MIN_SHIFT = 20;
 
 __device__ __forceinline__ float fx_scale(int max_occ, int ev) {
@@ -609,7 +614,7 @@ __device__ void finalize_public(const FitDev& f, int ctid, int nc, int* s_it) {
 //            is a private statistic, else 1)
 //   counts   uint32 [2 slots][window_max + 8]: the window's 16-bit click-count
 //            pairs of the k-th tile in slot k & 1, read by its M-step
-//   boost    uint8 [2 slots][window_max + 8]: b(a) of the k-th tile's window
+//   boost    uint8 [2 slots][window_max + 8]: e(a) of the k-th tile's window
 //            entries (fixed-point attractiveness bins) in slot k & 1
 //   stage s  { uint16 rel[10][spt_pad], uint16 clk[spt_pad],
 //              float atr[window_max + 8], float sat[window_max + 8] (DBN) }
@@ -678,9 +683,9 @@ em_fused_kernel(const FitDev* __restrict__ fits, const TileDev* __restrict__ til
     }
     for (int k = tid; k < MC_MAX_PUB; k += blockDim.x) { pub_acc[k] = 0.0; pub_tile[0][k] = 0.0f; pub_tile[1][k] = 0.0f; }
     for (int k = tid; k < (int)(2 * L.bins_buf); k += blockDim.x) bins[k] = 0.0f;
-    // Boost bytes start at 0: an entry without attractiveness adds keeps a
-    // byte <= kMaxBoost, so its M-step factor stays finite (its bin is 0).
-    for (int k = tid; k < (int)(2 * L.cnt_slot); k += blockDim.x) smem[L.boost_off + k] = 0;
+    // Boost bytes start at 126 (b = 0): an entry without attractiveness adds
+    // keeps a byte in [66, 255], so its M-step factor stays finite (its bin is 0).
+    for (int k = tid; k < (int)(2 * L.cnt_slot); k += blockDim.x) smem[L.boost_off + k] = 126;
     fence_async_shared();
     __syncthreads();
 
