@@ -64,6 +64,8 @@ def parse_args():
     ap.add_argument("--e2e-iters", type=int, default=50)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-train", action="store_true",
+                    help="adjoint workload: skip EM's curve and Adam (EM and adjoint timing, gradient error only)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
     ap.add_argument("--parity-iters", type=int, default=50,
@@ -621,15 +623,25 @@ def run_adjoint(args, rank: int, world: int, local: int):
     em.init_parameters(ds)
     em_curve = []
     t_em = 0.0
-    for it in range(50):
+    for it in range(0 if args.no_train else 50):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         em.em(1, IMPL_FUSED)
         torch.cuda.synchronize()
         t_em += time.perf_counter() - t0
         em_curve.append((t_em, em.evaluate(1).llh))
-    target = max(ll for _, ll in em_curve)  # EM's best test LL within 50 iterations
-    t_em_target = next(t for t, ll in em_curve if ll >= target - 1e-4 * abs(target))
+    target = max(ll for _, ll in em_curve) if em_curve else None  # EM's best test LL within 50 iterations
+    t_em_target = next(t for t, ll in em_curve if ll >= target - 1e-4 * abs(target)) if em_curve else None
+    # EM's own device time per iteration on these sessions (CUDA events, the
+    # fit's graph replay), for the per-session cost of the adjoint
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    em.em(64, IMPL_FUSED)
+    ev1.record()
+    torch.cuda.synchronize()
+    em_ms = ev0.elapsed_time(ev1) / 64
 
     # Adam's minibatches: consecutive ranges of a random order of whole
     # queries (unbiased, and the adjoint's tile path applies).
@@ -667,27 +679,64 @@ def run_adjoint(args, rank: int, world: int, local: int):
 
     batch = 262_144
     steps_per_epoch = (n_train + batch - 1) // batch
-    gradient.train_adam(trainer_model, n_qd, steps=20 * steps_per_epoch, batch=batch, lr=0.05, callback=cb,
-                        callback_every=steps_per_epoch, device=local)
+    if not args.no_train:
+        gradient.train_adam(trainer_model, n_qd, steps=20 * steps_per_epoch, batch=batch, lr=0.05, callback=cb,
+                            callback_every=steps_per_epoch, device=local)
     reach = next(((s, t, ll) for s, t, ll in curve if ll >= target - 1e-4 * abs(target)), None)
     t_steps = curve[-1][1] if curve else None
 
-    # adjoint throughput: one forward + backward over all training sessions
+    # adjoint throughput: one log-likelihood + gradient pass over all training
+    # sessions through the C-ABI (mc_dbn_loglik_grad: gradient clear, the tile
+    # kernel, FP32 conversion), and the same pass through the autograd wrapper
+    # (forward + backward), whose Python and autograd dispatch the GPU waits for
     a = torch.zeros(n_qd, device=dev, requires_grad=True)
     b = torch.zeros(n_qd, device=dev, requires_grad=True)
     g = torch.zeros(1, device=dev, requires_grad=True)
-    for _ in range(3):
+    da_, db_, dg_ = torch.empty_like(a), torch.empty_like(b), torch.empty_like(g)
+    ll_ = torch.empty((), dtype=torch.float64, device=dev)
+    stream_ = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def c_pass():
+        api.check(lib.mc_dbn_loglik_grad(trainer_model._h, 0, n_train, C.c_void_p(a.data_ptr()),
+                                         C.c_void_p(b.data_ptr()), C.c_void_p(g.data_ptr()), 0,
+                                         C.c_void_p(da_.data_ptr()), C.c_void_p(db_.data_ptr()),
+                                         C.c_void_p(dg_.data_ptr()), C.c_void_p(ll_.data_ptr()), stream_))
+
+    def autograd_pass():
         gradient.dbn_loglik(a, b, g, trainer_model).backward()
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    k = 10
-    for _ in range(k):
-        gradient.dbn_loglik(a, b, g, trainer_model).backward()
-    e1.record()
-    torch.cuda.synchronize()
-    ms_grad = e0.elapsed_time(e1) / k
+
+    def timed_ms(fn, k=10):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(k):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k
+
+    ms_grad = timed_ms(c_pass)
+    ms_autograd = timed_ms(autograd_pass)
+    # the FP32 gradient against the FP64 one at logits drawn N(-1, 1)
+    gen = torch.Generator(device="cpu").manual_seed(7)
+    a_init = (torch.randn(n_qd, generator=gen) - 1).to(dev)
+    b_init = (torch.randn(n_qd, generator=gen) - 1).to(dev)
+    grads = {}
+    for fp64 in (False, True):
+        a2 = a_init.clone().requires_grad_(True)
+        b2 = b_init.clone().requires_grad_(True)
+        g2 = torch.full((1,), 1.5, device=dev, requires_grad=True)
+        gradient.dbn_loglik(a2, b2, g2, trainer_model, fp64=fp64).backward()
+        grads[fp64] = (a2.grad.double(), b2.grad.double(), float(g2.grad))
+    grad_err = {}
+    for k_, i_ in (("alpha", 0), ("beta", 1)):
+        d_ = (grads[False][i_] - grads[True][i_]).abs()
+        grad_err[k_] = {"max_abs": float(d_.max()),
+                        "max_rel_floor1": float((d_ / grads[True][i_].abs().clamp_min(1.0)).max())}
+    grad_err["gamma_rel"] = abs(grads[False][2] - grads[True][2]) / abs(grads[True][2])
     if rank == 0:
         line = {
             "metric": "seconds for Adam to reach EM's best 50-iteration test LL (DBN, 5M sessions)",
@@ -696,14 +745,18 @@ def run_adjoint(args, rank: int, world: int, local: int):
             "config": {"workload": "DBN EM (fused, from the prior) vs Adam lr 0.05, batch 262,144 sessions",
                        "train_sessions": n_train, "n_qd": n_qd},
             "em": {"target_test_llh": target, "seconds_to_target": t_em_target, "seconds_50_iterations": t_em,
-                   "final_test_llh": em_curve[-1][1]},
+                   "final_test_llh": em_curve[-1][1] if em_curve else None},
             "adam": {"reached": reach is not None, "steps": reach[0] if reach else None,
                      "seconds": reach[1] if reach else None, "final_test_llh": curve[-1][2] if curve else None,
                      "best_test_llh": max(ll for _, _, ll in curve) if curve else None},
             "adam_ms_per_step": 1000.0 * t_steps / (20 * steps_per_epoch) if t_steps else None,
             "adjoint": {"ms_per_forward_backward": ms_grad,
+                        "autograd_ms_per_forward_backward": ms_autograd,
                         "session_gradients_per_s": n_train / (ms_grad / 1000.0),
-                        "em_session_iterations_per_s": n_train * 50 / t_em,
+                        "em_ms_per_iteration": em_ms,
+                        "forward_backward_over_em_iteration": ms_grad / em_ms,
+                        "fp32_gradient_vs_fp64": grad_err,
+                        "em_session_iterations_per_s": n_train * 50 / t_em if t_em else None,
                         "path": "tiles (sessions grouped by query, gradient summed per tile in shared memory)"},
         }
         print(json.dumps(line), flush=True)

@@ -110,6 +110,13 @@ struct AdjointArgs {
     const float* alpha;      // logits [n_qd]
     const float* beta;       // logits [n_qd]
     const float* gamma;      // logit [1]
+    const uint2* cnt;        // [n_qd] occurrences (x) of each pair in the training set
+    // Per staged tile t (tcnt_off[t] >= 0), per window entry i, at
+    // tcnt[tcnt_off[t] + i]: the counts over all of the tile's sessions of
+    // occurrences, occurrences at or before the session's last click, clicks
+    // and last clicks (adjoint_counts_kernel); null when not built.
+    const uint4* tcnt;
+    const int64_t* tcnt_off;
     double scale;            // gradient scale (the caller's grad_output)
     double* g_alpha;         // FP64 gradient accumulators
     double* g_beta;
@@ -123,6 +130,11 @@ cudaError_t launch_adjoint(const AdjointArgs& A, bool grad, bool fp64, int n_sm,
 cudaError_t launch_adjoint_tiles(const AdjointArgs& A, const TileDev* tiles, int t0, int t1, int window_max, bool grad,
                                  bool fp64, int n_sm, cudaStream_t st);
 cudaError_t launch_grad_to_float(const double* src, float* dst, int64_t n, int n_sm, cudaStream_t st);
+// The parameter-independent per-tile counts of AdjointArgs::tcnt for tiles
+// [0, n_tiles) (tiles with off[t] < 0 are skipped).
+cudaError_t launch_adjoint_counts(const TileDev* tiles, int n_tiles, int window_max, const int32_t* pidx,
+                                  const uint16_t* click, int64_t stride, const int64_t* off, uint4* out, int n_sm,
+                                  cudaStream_t st);
 
 }  // namespace mcd
 

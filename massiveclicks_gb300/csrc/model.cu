@@ -354,6 +354,14 @@ struct mc_model {
     int n_tiles = 0, n_splits = 0, grid = 0;
     bool tiles_ready = false;  // tiles built for the current shape (PBM/UBM build them only for batches)
     std::vector<int64_t> h_tile_begin;  // first session of each tile, ascending (adjoint range lookups)
+    // Adjoint per-tile counts (adjoint_counts_kernel): entry offset of each
+    // staged tile (-1 otherwise), built with the tiles; the counts themselves
+    // on the first FP32 adjoint call over the tiles.
+    std::vector<int64_t> h_adj_off;
+    int64_t adj_entries = 0;
+    int64_t* d_adj_off = nullptr;
+    uint4* d_adj_cnt = nullptr;
+    int64_t adj_bytes = 0;
     // Launch shapes of the count kernels (entry kernel; dense PBM kernel).
     CountShape count_shape{8, 256, 8};
     CountShape dense_shape{0, 256, 6};
@@ -417,6 +425,13 @@ struct mc_model {
         tile_bytes = 0;
         tiles_ready = false;
         h_tile_begin.clear();
+        settle(d_adj_off, d_adj_cnt);
+        dfree(d_adj_off);
+        dfree(d_adj_cnt);
+        bytes -= adj_bytes;
+        adj_bytes = 0;
+        h_adj_off.clear();
+        adj_entries = 0;
     }
 
     void free_plain() {
@@ -662,6 +677,10 @@ int mc_model::build_tiles() {
     h_tile_begin.resize(tiles.size());
     for (size_t i = 0; i < tiles.size(); i++) h_tile_begin[i] = tiles[i].s_begin;
     if (!std::is_sorted(h_tile_begin.begin(), h_tile_begin.end())) h_tile_begin.clear();  // no range lookups
+    h_adj_off.assign(tiles.size(), -1);
+    adj_entries = 0;
+    for (size_t i = 0; i < tiles.size(); i++)
+        if (tiles[i].qd_count <= wqd) { h_adj_off[i] = adj_entries; adj_entries += tiles[i].qd_count; }
     n_splits = (int)splits.size();
     split_bins_count = bin_off;
     int64_t before = bytes;
@@ -1791,6 +1810,9 @@ static AdjointArgs adjoint_args(mc_model* m, int64_t s_begin, int64_t s_count, c
     A.alpha = alpha;
     A.beta = beta;
     A.gamma = gamma;
+    A.cnt = m->d_cnt;
+    A.tcnt = nullptr;
+    A.tcnt_off = nullptr;
     A.scale = scale;
     A.g_alpha = m->d_grad;
     A.g_beta = m->d_grad + m->qd_alloc();
@@ -1801,8 +1823,36 @@ static AdjointArgs adjoint_args(mc_model* m, int64_t s_begin, int64_t s_count, c
 
 // Through the tiles when the sessions are grouped by query (tiles built),
 // else one thread per session with global atomics.
-static cudaError_t run_adjoint(mc_model* m, const AdjointArgs& A, bool grad, bool fp64, cudaStream_t st) {
+// The FP32 gradient's per-tile counts (adjoint_counts_kernel), built once per
+// tile layout on the first call that takes the tile path.
+static int ensure_adjoint_counts(mc_model* m, cudaStream_t st) {
+    if (!(m->fused_ok && m->tiles_ready && !m->h_tile_begin.empty()) || m->adj_entries == 0 || m->d_adj_cnt)
+        return MC_OK;
+    const int64_t before = m->bytes;
+    int rc = dalloc(&m->d_adj_off, m->h_adj_off.size(), &m->bytes);
+    if (!rc) rc = dalloc(&m->d_adj_cnt, (size_t)m->adj_entries, &m->bytes);
+    if (rc) {
+        dfree(m->d_adj_off);
+        dfree(m->d_adj_cnt);
+        m->bytes = before;
+        return rc;
+    }
+    m->adj_bytes = m->bytes - before;
+    CK(cudaMemcpyAsync(m->d_adj_off, m->h_adj_off.data(), m->h_adj_off.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
+                       st));
+    CK(launch_adjoint_counts(m->d_tiles, m->n_tiles, m->wqd, m->d_pidx, m->d_click, m->stride, m->d_adj_off,
+                             m->d_adj_cnt, m->n_sm, st));
+    CK(cudaStreamSynchronize(st));  // the host offsets stay alive meanwhile
+    return MC_OK;
+}
+
+static cudaError_t run_adjoint(mc_model* m, const AdjointArgs& A0, bool grad, bool fp64, cudaStream_t st) {
+    AdjointArgs A = A0;
     if (m->fused_ok && m->tiles_ready && !m->h_tile_begin.empty()) {
+        if (grad && !fp64 && m->d_adj_cnt) {
+            A.tcnt = m->d_adj_cnt;
+            A.tcnt_off = m->d_adj_off;
+        }
         const auto& tb = m->h_tile_begin;
         // tiles [t0, t1) intersect [begin, begin + count): tile starts ascend
         int t0 = (int)(std::upper_bound(tb.begin(), tb.end(), A.begin) - tb.begin()) - 1;
@@ -1836,6 +1886,7 @@ extern "C" int mc_dbn_loglik_backward(mc_model* m, int64_t s_begin, int64_t s_co
     cudaStream_t st = m->pick(stream);
     AdjointArgs A = adjoint_args(m, s_begin, s_count, alpha, beta, gamma, grad_output);
     CK(cudaMemsetAsync(m->d_grad, 0, (size_t)(2 * m->qd_alloc() + 2) * 8, st));
+    if (!fp64 && (rc = ensure_adjoint_counts(m, st))) return rc;
     CK(run_adjoint(m, A, true, fp64 != 0, st));
     CK(launch_grad_to_float(A.g_alpha, d_alpha, m->n_qd, m->n_sm, st));
     CK(launch_grad_to_float(A.g_beta, d_beta, m->n_qd, m->n_sm, st));
@@ -1858,6 +1909,7 @@ extern "C" int mc_dbn_loglik_grad(mc_model* m, int64_t s_begin, int64_t s_count,
     cudaStream_t st = m->pick(stream);
     AdjointArgs A = adjoint_args(m, s_begin, s_count, alpha, beta, gamma, 1.0);
     CK(cudaMemsetAsync(m->d_grad, 0, (size_t)(2 * m->qd_alloc() + 2) * 8, st));
+    if (!fp64 && (rc = ensure_adjoint_counts(m, st))) return rc;
     CK(run_adjoint(m, A, true, fp64 != 0, st));
     CK(launch_grad_to_float(A.g_alpha, d_alpha, m->n_qd, m->n_sm, st));
     CK(launch_grad_to_float(A.g_beta, d_beta, m->n_qd, m->n_sm, st));

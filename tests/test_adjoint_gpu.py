@@ -153,6 +153,39 @@ def test_fp32_gradient_close_to_fp64():
     assert g32 == pytest.approx(g64, rel=1e-4)
 
 
+def _grads_range(cm, al, be, ga, begin, count, fp64=False):
+    dev = torch.device("cuda", 0)
+    a = torch.tensor(al, device=dev, requires_grad=True)
+    b = torch.tensor(be, device=dev, requires_grad=True)
+    g = torch.tensor(ga, device=dev, requires_grad=True)
+    ll = gradient.dbn_loglik(a, b, g, cm, begin, count, fp64=fp64)
+    ll.backward()
+    return a.grad.cpu().numpy().astype(np.float64), b.grad.cpu().numpy().astype(np.float64), \
+        float(g.grad.cpu().numpy()[0])
+
+
+def test_fp32_counted_terms_whole_and_cut_tiles():
+    """The FP32 tile path counts the constant terms (clicked ranks, unclicked
+    ranks before the last click): from the per-tile counts for a tile wholly
+    inside the called range, with atomics for a tile the range cuts.  The
+    gradient over all training sessions equals the sum over two ranges split
+    inside tiles, and both match FP64 at the FP32 bar."""
+    case, cm, al, be, ga = _setup("dbn_ccmclicks", seed=8)
+    n = cm.n_train
+    a_all, b_all, g_all = _grads_range(cm, al, be, ga, 0, n)
+    cut = n // 2 + 17
+    a1, b1, g1 = _grads_range(cm, al, be, ga, 0, cut)
+    a2, b2, g2 = _grads_range(cm, al, be, ga, cut, n - cut)
+    a64, b64, g64 = _grads_range(cm, al, be, ga, 0, n, fp64=True)
+    np.testing.assert_allclose(a1 + a2, a_all, rtol=2e-5, atol=2e-5)
+    np.testing.assert_allclose(b1 + b2, b_all, rtol=2e-5, atol=2e-5)
+    assert g1 + g2 == pytest.approx(g_all, rel=1e-5)
+    for got in (a_all, a1 + a2):
+        np.testing.assert_allclose(got, a64, rtol=1e-4, atol=1e-5)
+    for got in (b_all, b1 + b2):
+        np.testing.assert_allclose(got, b64, rtol=1e-4, atol=1e-5)
+
+
 def test_ranges_add_up():
     case, cm, al, be, ga = _setup(seed=5)
     dev = torch.device("cuda", 0)
