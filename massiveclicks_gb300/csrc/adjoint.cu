@@ -303,6 +303,9 @@ __device__ __forceinline__ void adjoint_sessions(const AdjointArgs& A, const Adj
                 } else if constexpr (KIND != kAdjGlobal) {
                     atomicAdd(W.bins + rl[r], (Bin)(w * (T(1) - ar)));
                     atomicAdd(W.bins + W.wcap + rl[r], (Bin)(w * db));
+                } else if (sizeof(T) == 4 && A.f_alpha) {
+                    atomicAdd(A.f_alpha + rl[r], (float)(w * (T(1) - ar)));
+                    atomicAdd(A.f_beta + rl[r], (float)(w * db));
                 } else {
                     atomicAdd(A.g_alpha + rl[r], (double)(w * (T(1) - ar)));
                     atomicAdd(A.g_beta + rl[r], (double)(w * db));
@@ -323,6 +326,8 @@ __device__ __forceinline__ void adjoint_sessions(const AdjointArgs& A, const Adj
                     }
                 } else if constexpr (KIND != kAdjGlobal) {
                     atomicAdd(W.bins + rl[r], (Bin)(w * da));
+                } else if (sizeof(T) == 4 && A.f_alpha) {
+                    atomicAdd(A.f_alpha + rl[r], (float)(w * da));
                 } else {
                     atomicAdd(A.g_alpha + rl[r], (double)(w * da));
                 }
@@ -452,7 +457,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) adjoint_tiles_ker
                 for (int i = threadIdx.x; i < tile.qd_count; i += blockDim.x) {
                     const int64_t q = tile.qd_begin + i;
                     // the entry's bins, summed over the copies of a small window
-                    long long sum[NB];
+                    // (32-bit: the bound on an entry's adds covers all copies)
+                    int sum[NB];
                     double dsum[NB];
                     for (int k = 0; k < NB; k++) { sum[k] = 0; dsum[k] = 0.0; }
                     if (small) {
@@ -470,6 +476,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) adjoint_tiles_ker
                         }
                     }
                     double sa = dsum[0], sb = dsum[1];
+                    float fa_out = 0.0f, fb_out = 0.0f;
                     if constexpr (FX) {
                         // 2^-sh and 2^-(sh + b) (exact), the counted terms, the caller's scale
                         const float a = va[i], sv = vs[i];
@@ -478,10 +485,20 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) adjoint_tiles_ker
                         const float nc = (float)sum[2], nl = (float)sum[3], nb = (float)sum[4];
                         const float fa = (float)sum[0] * inv_a + (nc - a * nb);
                         const float fb = (float)sum[1] * inv_b - (nc - nl) * sv;
-                        sa = (double)(w * fa);
-                        sb = (double)(w * fb);
+                        fa_out = w * fa;
+                        fb_out = w * fb;
+                        sa = (double)fa_out;
+                        sb = (double)fb_out;
                     }
-                    if (owned) {
+                    if (FX && A.f_alpha) {
+                        if (owned) {
+                            A.f_alpha[q] = fa_out;
+                            A.f_beta[q] = fb_out;
+                        } else {
+                            if (fa_out != 0.0f) atomicAdd(A.f_alpha + q, fa_out);
+                            if (fb_out != 0.0f) atomicAdd(A.f_beta + q, fb_out);
+                        }
+                    } else if (owned) {
                         A.g_alpha[q] = sa;
                         A.g_beta[q] = sb;
                     } else {

@@ -120,6 +120,10 @@ struct AdjointArgs {
     double scale;            // gradient scale (the caller's grad_output)
     double* g_alpha;         // FP64 gradient accumulators
     double* g_beta;
+    // FP32 tile path: the alpha and beta gradients written straight into these
+    // (cleared by the caller) instead of g_alpha, g_beta; null otherwise.
+    float* f_alpha;
+    float* f_beta;
     double* g_gamma;
     double* ll_out;          // log-likelihood sum
 };

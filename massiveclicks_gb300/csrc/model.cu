@@ -1813,6 +1813,8 @@ static AdjointArgs adjoint_args(mc_model* m, int64_t s_begin, int64_t s_count, c
     A.cnt = m->d_cnt;
     A.tcnt = nullptr;
     A.tcnt_off = nullptr;
+    A.f_alpha = nullptr;
+    A.f_beta = nullptr;
     A.scale = scale;
     A.g_alpha = m->d_grad;
     A.g_beta = m->d_grad + m->qd_alloc();
@@ -1823,11 +1825,15 @@ static AdjointArgs adjoint_args(mc_model* m, int64_t s_begin, int64_t s_count, c
 
 // Through the tiles when the sessions are grouped by query (tiles built),
 // else one thread per session with global atomics.
+// Sessions grouped by query with tiles built: the adjoint's tile path.
+static bool adjoint_tile_path(const mc_model* m) {
+    return m->fused_ok && m->tiles_ready && !m->h_tile_begin.empty();
+}
+
 // The FP32 gradient's per-tile counts (adjoint_counts_kernel), built once per
 // tile layout on the first call that takes the tile path.
 static int ensure_adjoint_counts(mc_model* m, cudaStream_t st) {
-    if (!(m->fused_ok && m->tiles_ready && !m->h_tile_begin.empty()) || m->adj_entries == 0 || m->d_adj_cnt)
-        return MC_OK;
+    if (!adjoint_tile_path(m) || m->adj_entries == 0 || m->d_adj_cnt) return MC_OK;
     const int64_t before = m->bytes;
     int rc = dalloc(&m->d_adj_off, m->h_adj_off.size(), &m->bytes);
     if (!rc) rc = dalloc(&m->d_adj_cnt, (size_t)m->adj_entries, &m->bytes);
@@ -1846,9 +1852,39 @@ static int ensure_adjoint_counts(mc_model* m, cudaStream_t st) {
     return MC_OK;
 }
 
+// Gradient outputs.  The FP32 tile path writes the alpha and beta gradients
+// straight into the caller's FP32 arrays (cleared here); the FP64 and
+// per-session paths accumulate in the model's FP64 arrays, converted after.
+// The gamma gradient and the log-likelihood are FP64 in both.
+static int adjoint_outputs(mc_model* m, AdjointArgs& A, bool fp64, float* d_alpha, float* d_beta, cudaStream_t st) {
+    if (!fp64 && adjoint_tile_path(m)) {
+        int rc = ensure_adjoint_counts(m, st);
+        if (rc) return rc;
+        CK(cudaMemsetAsync(d_alpha, 0, (size_t)m->n_qd * 4, st));
+        CK(cudaMemsetAsync(d_beta, 0, (size_t)m->n_qd * 4, st));
+        CK(cudaMemsetAsync(A.g_gamma, 0, 2 * 8, st));  // g_gamma, ll_out
+        A.f_alpha = d_alpha;
+        A.f_beta = d_beta;
+        return MC_OK;
+    }
+    CK(cudaMemsetAsync(m->d_grad, 0, (size_t)(2 * m->qd_alloc() + 2) * 8, st));
+    return MC_OK;
+}
+
+static cudaError_t adjoint_finish(mc_model* m, const AdjointArgs& A, float* d_alpha, float* d_beta, float* d_gamma,
+                                  cudaStream_t st) {
+    cudaError_t e = cudaSuccess;
+    if (!A.f_alpha) {
+        e = launch_grad_to_float(A.g_alpha, d_alpha, m->n_qd, m->n_sm, st);
+        if (e == cudaSuccess) e = launch_grad_to_float(A.g_beta, d_beta, m->n_qd, m->n_sm, st);
+    }
+    if (e == cudaSuccess) e = launch_grad_to_float(A.g_gamma, d_gamma, 1, m->n_sm, st);
+    return e;
+}
+
 static cudaError_t run_adjoint(mc_model* m, const AdjointArgs& A0, bool grad, bool fp64, cudaStream_t st) {
     AdjointArgs A = A0;
-    if (m->fused_ok && m->tiles_ready && !m->h_tile_begin.empty()) {
+    if (adjoint_tile_path(m)) {
         if (grad && !fp64 && m->d_adj_cnt) {
             A.tcnt = m->d_adj_cnt;
             A.tcnt_off = m->d_adj_off;
@@ -1885,12 +1921,9 @@ extern "C" int mc_dbn_loglik_backward(mc_model* m, int64_t s_begin, int64_t s_co
     if (!d_alpha || !d_beta || !d_gamma) return set_error(MC_ERR_INVALID, "dbn_loglik_backward: null gradient output");
     cudaStream_t st = m->pick(stream);
     AdjointArgs A = adjoint_args(m, s_begin, s_count, alpha, beta, gamma, grad_output);
-    CK(cudaMemsetAsync(m->d_grad, 0, (size_t)(2 * m->qd_alloc() + 2) * 8, st));
-    if (!fp64 && (rc = ensure_adjoint_counts(m, st))) return rc;
+    if ((rc = adjoint_outputs(m, A, fp64 != 0, d_alpha, d_beta, st))) return rc;
     CK(run_adjoint(m, A, true, fp64 != 0, st));
-    CK(launch_grad_to_float(A.g_alpha, d_alpha, m->n_qd, m->n_sm, st));
-    CK(launch_grad_to_float(A.g_beta, d_beta, m->n_qd, m->n_sm, st));
-    CK(launch_grad_to_float(A.g_gamma, d_gamma, 1, m->n_sm, st));
+    CK(adjoint_finish(m, A, d_alpha, d_beta, d_gamma, st));
     if (loglik) {
         CK(cudaMemcpyAsync(loglik, A.ll_out, 8, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
@@ -1908,12 +1941,9 @@ extern "C" int mc_dbn_loglik_grad(mc_model* m, int64_t s_begin, int64_t s_count,
     if (!d_alpha || !d_beta || !d_gamma || !d_loglik) return set_error(MC_ERR_INVALID, "dbn_loglik_grad: null output");
     cudaStream_t st = m->pick(stream);
     AdjointArgs A = adjoint_args(m, s_begin, s_count, alpha, beta, gamma, 1.0);
-    CK(cudaMemsetAsync(m->d_grad, 0, (size_t)(2 * m->qd_alloc() + 2) * 8, st));
-    if (!fp64 && (rc = ensure_adjoint_counts(m, st))) return rc;
+    if ((rc = adjoint_outputs(m, A, fp64 != 0, d_alpha, d_beta, st))) return rc;
     CK(run_adjoint(m, A, true, fp64 != 0, st));
-    CK(launch_grad_to_float(A.g_alpha, d_alpha, m->n_qd, m->n_sm, st));
-    CK(launch_grad_to_float(A.g_beta, d_beta, m->n_qd, m->n_sm, st));
-    CK(launch_grad_to_float(A.g_gamma, d_gamma, 1, m->n_sm, st));
+    CK(adjoint_finish(m, A, d_alpha, d_beta, d_gamma, st));
     CK(cudaMemcpyAsync(d_loglik, A.ll_out, 8, cudaMemcpyDeviceToDevice, st));
     if (!stream) CK(cudaStreamSynchronize(st));
     return MC_OK;
