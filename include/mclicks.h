@@ -248,7 +248,9 @@ int mc_model_memory(const mc_model* m, int64_t* bytes);
 /* Device blocks the library freed are kept in a per-device cache and handed
  * out again (models created and destroyed with the same sizes then skip
  * cudaMalloc / cudaFree).  mc_empty_cache frees the cached blocks of one device
- * (-1: all) back to the driver; mc_cache_bytes reports how much is cached. */
+ * (-1: all, and also the page-locked host buffers kept for upload readbacks)
+ * back to the driver; mc_cache_bytes reports how much device memory is
+ * cached. */
 int mc_empty_cache(int device, int64_t* bytes_released);
 int mc_cache_bytes(int device, int64_t* bytes);
 

@@ -20,6 +20,8 @@ std::mutex g_mu;
 std::unordered_map<void*, Block> g_live;                 // handed out
 std::map<std::pair<int, size_t>, std::vector<void*>> g_free;  // (device, size) -> cached blocks
 size_t g_cached = 0;
+std::unordered_map<void*, size_t> g_host_live;            // page-locked blocks handed out
+std::map<size_t, std::vector<void*>> g_host_free;          // size -> cached page-locked blocks
 
 // 512 B granularity below 1 MiB, 2 MiB above: repeated uploads of one data set
 // ask for identical sizes, and nearby sizes share a class.
@@ -32,6 +34,11 @@ size_t round_size(size_t b) {
 
 size_t release_locked(int device) {
     size_t freed = 0;
+    if (device < 0) {
+        for (auto& kv : g_host_free)
+            for (void* p : kv.second) cudaFreeHost(p);
+        g_host_free.clear();
+    }
     for (auto it = g_free.begin(); it != g_free.end();) {
         if (device >= 0 && it->first.first != device) { ++it; continue; }
         int cur = 0;
@@ -85,6 +92,35 @@ void dev_free(void* p) {
     g_free[{it->second.device, it->second.size}].push_back(p);
     g_cached += it->second.size;
     g_live.erase(it);
+}
+
+cudaError_t host_alloc(void** p, size_t bytes) {
+    *p = nullptr;
+    const size_t size = round_size(bytes);
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_host_free.find(size);
+    if (it != g_host_free.end() && !it->second.empty()) {
+        *p = it->second.back();
+        it->second.pop_back();
+        g_host_live[*p] = size;
+        return cudaSuccess;
+    }
+    cudaError_t e = cudaHostAlloc(p, size, cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return e;
+    }
+    g_host_live[*p] = size;
+    return cudaSuccess;
+}
+
+void host_free(void* p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_host_live.find(p);
+    if (it == g_host_live.end()) return;
+    g_host_free[it->second].push_back(p);
+    g_host_live.erase(it);
 }
 
 size_t dev_cache_release(int device) {

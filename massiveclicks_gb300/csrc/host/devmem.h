@@ -32,6 +32,14 @@ size_t dev_cache_release(int device);
 // Bytes held in the cache of one device (-1: every device).
 size_t dev_cache_bytes(int device);
 
+// Page-locked host memory through the same kind of cache (one pool for every
+// device): the readbacks of an upload go to page-locked buffers, which the
+// driver copies into directly, and page-locking them anew for every model
+// would cost more than the copies.  host_free returns a block to the pool;
+// dev_cache_release(-1) also frees the pool's cached blocks.
+cudaError_t host_alloc(void** p, size_t bytes);
+void host_free(void* p);
+
 }  // namespace mch
 
 #endif

@@ -324,15 +324,45 @@ struct ParamDesc {
 // upload pass runs on each chunk as soon as it has landed.
 static const int kUploadChunks = 8;
 
+// A host array in page-locked memory from the library's pool (mch::host_alloc):
+// upload readbacks land in it directly.  resize keeps no contents.
+template <class T>
+struct PinnedArray {
+    T* p = nullptr;
+    size_t n = 0, cap = 0;
+    PinnedArray() = default;
+    PinnedArray(const PinnedArray&) = delete;
+    PinnedArray& operator=(const PinnedArray&) = delete;
+    ~PinnedArray() { mch::host_free(p); }
+    cudaError_t resize(size_t m) {
+        if (m > cap) {
+            mch::host_free(p);
+            p = nullptr;
+            n = cap = 0;
+            void* q = nullptr;
+            cudaError_t e = mch::host_alloc(&q, std::max<size_t>(m, 1) * sizeof(T));
+            if (e != cudaSuccess) return e;
+            p = static_cast<T*>(q);
+            cap = m;
+        }
+        n = m;
+        return cudaSuccess;
+    }
+    size_t size() const { return n; }
+    T& operator[](size_t i) { return p[i]; }
+    const T& operator[](size_t i) const { return p[i]; }
+    T* data() { return p; }
+};
+
 struct mc_model {
     int model = 0, mode = 0, device = 0, n_pub = 0, n_sm = 0;
     int64_t n = 0, stride = 0, n_qd = 0, bytes = 0;
     bool uploaded = false, fused_ok = false;
     std::string fused_reason;
     // query segments of the training set: sessions and qd range
-    std::vector<int64_t> seg_begin;
-    std::vector<int32_t> seg_lo, seg_hi;  // qd range [lo, hi) of each segment, as the upload pass finds it
-    std::vector<uint32_t> packbits;  // bit s: training session s has a click
+    PinnedArray<int64_t> seg_begin;
+    PinnedArray<int32_t> seg_lo, seg_hi;  // qd range [lo, hi) of each segment, as the upload pass finds it
+    PinnedArray<uint32_t> packbits;  // bit s: training session s has a click
     int spt = 1024, wqd = 1536, block = 256, stages = 2, ctas_per_sm = 1;
     // fused state
     int32_t* d_pidx = nullptr;
@@ -823,15 +853,24 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     m->n_qd = n_qd;
     m->stride = std::max<int64_t>(32, (n + 31) / 32 * 32);
 
-    // The session indices and clicks go up on a side stream, in chunks, while
-    // the query segments are found on st; the upload pass then runs on each
-    // chunk as its copy lands.  The side stream first waits for the work
-    // already queued on st (which may still be writing the host buffers).
+    // The query ids go up first, on st, so that the query segments are found
+    // while the session indices and clicks follow on a side stream, in
+    // chunks; the upload pass then runs on each chunk as its copy lands.  (With
+    // the query copy queued behind the chunks, it landed last and every chunk's
+    // upload pass waited for the end of the copies.)  The side stream first
+    // waits for the work already queued on st (which may still be writing the
+    // host buffers) and for the query copy.
     int rc;
     int32_t* d_src = nullptr;
+    int32_t* d_q = nullptr;
     int64_t scratch = 0;
     if ((rc = dalloc(&d_src, (size_t)std::max<int64_t>(n * MC_R, 1), &scratch))) return rc;
     if ((rc = dalloc(&m->d_click, (size_t)std::max<int64_t>(n, 1), &m->bytes))) { dfree(d_src); return rc; }
+    if ((rc = dalloc(&d_q, (size_t)std::max<int64_t>(n, 1), &scratch))) { dfree(d_src); return rc; }
+    if (n) {
+        cudaError_t eq = cudaMemcpyAsync(d_q, query, (size_t)n * 4, cudaMemcpyHostToDevice, st);
+        if (eq != cudaSuccess) { dfree(d_src); dfree(d_q); m->free_train(); return cuda_fail("model_upload", eq); }
+    }
     int n_chunks = 0;
     int64_t chunk_at[kUploadChunks + 1] = {0};
     if (n) {
@@ -852,7 +891,9 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
         }
         if (ec != cudaSuccess) {
             cudaStreamSynchronize(cs);
+            cudaStreamSynchronize(st);
             dfree(d_src);
+            dfree(d_q);
             m->free_train();
             return cuda_fail("model_upload", ec);
         }
@@ -866,7 +907,6 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     // Query segments (runs of equal query id), found on the device: block
     // counts, their prefix on the host, then seg_begin and each session's
     // segment index.
-    int32_t* d_q = nullptr;
     int32_t* d_seg_id = nullptr;
     int64_t* d_seg_begin = nullptr;
     int64_t n_seg = 0;
@@ -877,8 +917,7 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
         int64_t* d_off = nullptr;
         int rc0;
         auto free0 = [&]() { dfree(d_blk); dfree(d_off); };
-        if ((rc0 = dalloc(&d_q, (size_t)std::max<int64_t>(n, 1), &scratch0)) ||
-            (rc0 = dalloc(&d_seg_id, (size_t)std::max<int64_t>(n, 1), &scratch0)) ||
+        if ((rc0 = dalloc(&d_seg_id, (size_t)std::max<int64_t>(n, 1), &scratch0)) ||
             (rc0 = dalloc(&d_blk, (size_t)std::max<int64_t>(nb, 1), &scratch0)) ||
             (rc0 = dalloc(&d_off, (size_t)std::max<int64_t>(nb, 1), &scratch0))) {
             drain();
@@ -890,7 +929,6 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
         cudaError_t e0 = cudaSuccess;
         auto ck0 = [&](cudaError_t x) { if (e0 == cudaSuccess) e0 = x; };
         if (n) {
-            ck0(cudaMemcpyAsync(d_q, query, (size_t)n * 4, cudaMemcpyHostToDevice, st));
             seg_count_kernel<<<(unsigned)nb, kSegBlock / 8, 0, st>>>(n, d_q, d_blk);
             ck0(cudaGetLastError());
             ck0(cudaMemcpyAsync(blk.data(), d_blk, (size_t)nb * 4, cudaMemcpyDeviceToHost, st));
@@ -905,8 +943,10 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
             seg_write_kernel<<<(unsigned)nb, kSegBlock / 8, 0, st>>>(n, d_q, d_off, d_seg_begin, d_seg_id);
             ck0(cudaGetLastError());
         }
-        m->seg_begin.assign((size_t)n_seg + 1, n);
-        if (n_seg) ck0(cudaMemcpyAsync(m->seg_begin.data(), d_seg_begin, (size_t)n_seg * 8, cudaMemcpyDeviceToHost, st));
+        ck0(m->seg_begin.resize((size_t)n_seg + 1));
+        if (e0 == cudaSuccess) m->seg_begin[(size_t)n_seg] = n;
+        if (n_seg && e0 == cudaSuccess)
+            ck0(cudaMemcpyAsync(m->seg_begin.data(), d_seg_begin, (size_t)n_seg * 8, cudaMemcpyDeviceToHost, st));
         ck0(cudaStreamSynchronize(st));
         free0();
         dfree(d_q);
@@ -999,11 +1039,12 @@ extern "C" int mc_model_upload(mc_model* m, int64_t n, const int32_t* query, con
     std::vector<unsigned long long> pub_counts(MC_PUB_COUNTS, 0);
     ck(cudaMemcpyAsync(flags, d_flag, 8, cudaMemcpyDeviceToHost, st));
     ck(cudaMemcpyAsync(pub_counts.data(), d_pub_counts, pub_counts.size() * 8, cudaMemcpyDeviceToHost, st));
-    m->packbits.assign((size_t)n_words, 0u);
-    if (n_words) ck(cudaMemcpyAsync(m->packbits.data(), d_packbits, (size_t)n_words * 4, cudaMemcpyDeviceToHost, st));
-    m->seg_lo.resize((size_t)n_seg);
-    m->seg_hi.resize((size_t)n_seg);
-    if (n_seg) {
+    ck(m->packbits.resize((size_t)n_words));
+    if (n_words && e == cudaSuccess)
+        ck(cudaMemcpyAsync(m->packbits.data(), d_packbits, (size_t)n_words * 4, cudaMemcpyDeviceToHost, st));
+    ck(m->seg_lo.resize((size_t)n_seg));
+    ck(m->seg_hi.resize((size_t)n_seg));
+    if (n_seg && e == cudaSuccess) {
         ck(cudaMemcpyAsync(m->seg_lo.data(), d_seg_lo, (size_t)n_seg * 4, cudaMemcpyDeviceToHost, st));
         ck(cudaMemcpyAsync(m->seg_hi.data(), d_seg_hi, (size_t)n_seg * 4, cudaMemcpyDeviceToHost, st));
     }
