@@ -208,7 +208,8 @@ struct AdjointBin<float> { using type = int; };
 enum AdjointTileKind { kAdjSmall = 0, kAdjWide = 1, kAdjGlobal = 2 };
 
 // A tile's view for its sessions: window values and scales, this thread's
-// bins (array k at bins + k * wcap), the tile's first window pair.
+// bins (array k at bins + k * wcap), the tile's first window pair, and its
+// packed sessions in click-mask order (prel [10][spad], pclk [spad]).
 template <typename T>
 struct AdjointTile {
     const T* va;
@@ -218,44 +219,56 @@ struct AdjointTile {
     typename AdjointBin<T>::type* bins;
     int wcap;
     int qd_begin, qd_count;
+    const uint16_t* prel;
+    const uint16_t* pclk;
+    int spad;
 };
 
 // The sessions [s0, s1) of one tile, one thread per session: the forward
 // recursion (log-likelihood) and, if grad, the reverse pass into the tile's
-// bins.  KIND and COUNT (FP32 counted terms by atomics: a tile cut by the
-// called range) are template parameters, so that the unrolled loop of each
-// kind carries no branch on the kind and stays small in the instruction cache.
-template <typename T, int KIND, bool COUNT>
+// bins.  KIND, COUNT (FP32 counted terms by atomics: a tile cut by the called
+// range) and PACKED (the tile's sessions read from its packed copy, in
+// click-mask order, so that the lanes of a warp take the same branches) are
+// template parameters, so that the unrolled loop of each kind carries no
+// branch on the kind and stays small in the instruction cache.
+template <typename T, int KIND, bool COUNT, bool PACKED>
 __device__ __forceinline__ void adjoint_sessions(const AdjointArgs& A, const AdjointTile<T>& W, int64_t s0,
                                                  int64_t s1, T g, T w, bool grad, T& lls_tile, T& g_bar_acc) {
     constexpr bool FX = sizeof(T) == 4 && KIND != kAdjGlobal;  // counted terms and fixed-point bins
     using Bin = typename AdjointBin<T>::type;
     auto a_of = [&](int rl) -> T { return KIND == kAdjGlobal ? sigm<T>(A.alpha[rl]) : W.va[rl]; };
     auto s_of = [&](int rl) -> T { return KIND == kAdjGlobal ? sigm<T>(A.beta[rl]) : W.vs[rl]; };
+    // Session k of the tile's range: its indices (window entries when packed)
+    // and clicks.
+    auto load = [&](int64_t k, int (&p)[MC_R], unsigned& m) {
+        if constexpr (PACKED) {
+            m = W.pclk[k];
+#pragma unroll
+            for (int r = 0; r < MC_R; r++) p[r] = W.prel[r * W.spad + k];
+        } else {
+            m = A.click[s0 + k];
+#pragma unroll
+            for (int r = 0; r < MC_R; r++) p[r] = A.pidx[(int64_t)r * A.stride + s0 + k];
+        }
+    };
     // Each thread loads its next session's indices and clicks while it works
     // on the current one (global loads are the longest wait here).
+    const int64_t n = s1 - s0;
     int pn[MC_R];
     unsigned mn = 0;
-    if (s0 + threadIdx.x < s1) {
-        mn = A.click[s0 + threadIdx.x];
-#pragma unroll
-        for (int r = 0; r < MC_R; r++) pn[r] = A.pidx[(int64_t)r * A.stride + s0 + threadIdx.x];
-    }
-    for (int64_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+    if (threadIdx.x < n) load(threadIdx.x, pn, mn);
+    for (int64_t k = threadIdx.x; k < n; k += blockDim.x) {
         int rl[MC_R];
         T ex[MC_R + 1], ip[MC_R];  // ip: 1 / p of unclicked ranks
         const unsigned m = mn;
         // A tile's sessions show only its window's pairs (the tiles are built
-        // so); the clamp keeps shared-memory accesses in bounds regardless.
-        // rl is the window entry, or the pair for a window too wide to stage.
+        // so, and the packing checked it); the clamp keeps shared-memory
+        // accesses in bounds regardless.  rl is the window entry, or the pair
+        // for a window too wide to stage.
 #pragma unroll
         for (int r = 0; r < MC_R; r++)
-            rl[r] = KIND == kAdjGlobal ? pn[r] : min(max(pn[r] - W.qd_begin, 0), W.qd_count - 1);
-        if (s + blockDim.x < s1) {
-            mn = A.click[s + blockDim.x];
-#pragma unroll
-            for (int r = 0; r < MC_R; r++) pn[r] = A.pidx[(int64_t)r * A.stride + s + blockDim.x];
-        }
+            rl[r] = KIND == kAdjGlobal || PACKED ? pn[r] : min(max(pn[r] - W.qd_begin, 0), W.qd_count - 1);
+        if (k + blockDim.x < n) load(k + blockDim.x, pn, mn);
         T a[MC_R], sv[MC_R];
 #pragma unroll
         for (int r = 0; r < MC_R; r++) {
@@ -337,14 +350,16 @@ __device__ __forceinline__ void adjoint_sessions(const AdjointArgs& A, const Adj
     }
 }
 
-// The rare kinds out of line: a window too wide to stage, and the tiles a
-// called range cuts (at most two per call), which count with atomics.  Only
-// the two hot loops are inlined into the kernel; with all five inlined, the
-// kernel spilled at its 80-register bound.
+// The rare kinds out of line: a window too wide to stage, the tiles a called
+// range cuts (at most two per call; they count with atomics), forward-only
+// calls and the FP64 instantiation (session order).  Only the two hot loops,
+// whole staged tiles from their packed copies, are inlined into the kernel;
+// with every kind inlined, the loop fell out of the instruction cache and the
+// kernel spilled.
 template <typename T, int KIND, bool COUNT>
 __device__ __noinline__ void adjoint_sessions_cold(const AdjointArgs& A, const AdjointTile<T>& W, int64_t s0,
                                                    int64_t s1, T g, T w, bool grad, T& lls_tile, T& g_bar_acc) {
-    adjoint_sessions<T, KIND, COUNT>(A, W, s0, s1, g, w, grad, lls_tile, g_bar_acc);
+    adjoint_sessions<T, KIND, COUNT, false>(A, W, s0, s1, g, w, grad, lls_tile, g_bar_acc);
 }
 
 // Four 256-thread blocks per SM in FP32 (at most 64 registers; the out-of-line
@@ -438,14 +453,26 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) adjoint_tiles_ker
         W.wcap = wcap;
         W.qd_begin = (int)tile.qd_begin;
         W.qd_count = tile.qd_count;
+        W.prel = nullptr;
+        W.pclk = nullptr;
+        W.spad = 0;
         T lls = T(0);
-        const bool count = FX && staged && !full;
+        const bool count = FX && staged && !full && grad;
+        const bool packed = FX && staged && full && A.pblk;
+        if (packed) {
+            const TileDev pt = A.ptiles[t];
+            W.prel = reinterpret_cast<const uint16_t*>(A.pblk + pt.blk_off);
+            W.spad = (tile.s_count + 7) & ~7;
+            W.pclk = W.prel + 10 * W.spad;
+        }
         if (small) {
-            if (count) adjoint_sessions_cold<T, kAdjSmall, true>(A, W, s0, s1, g, w, grad, lls, g_bar_acc);
-            else adjoint_sessions<T, kAdjSmall, false>(A, W, s0, s1, g, w, grad, lls, g_bar_acc);
+            if (packed) adjoint_sessions<T, kAdjSmall, false, true>(A, W, s0, s1, g, w, grad, lls, g_bar_acc);
+            else if (count) adjoint_sessions_cold<T, kAdjSmall, true>(A, W, s0, s1, g, w, grad, lls, g_bar_acc);
+            else adjoint_sessions_cold<T, kAdjSmall, false>(A, W, s0, s1, g, w, grad, lls, g_bar_acc);
         } else if (staged) {
-            if (count) adjoint_sessions_cold<T, kAdjWide, true>(A, W, s0, s1, g, w, grad, lls, g_bar_acc);
-            else adjoint_sessions<T, kAdjWide, false>(A, W, s0, s1, g, w, grad, lls, g_bar_acc);
+            if (packed) adjoint_sessions<T, kAdjWide, false, true>(A, W, s0, s1, g, w, grad, lls, g_bar_acc);
+            else if (count) adjoint_sessions_cold<T, kAdjWide, true>(A, W, s0, s1, g, w, grad, lls, g_bar_acc);
+            else adjoint_sessions_cold<T, kAdjWide, false>(A, W, s0, s1, g, w, grad, lls, g_bar_acc);
         } else {
             adjoint_sessions_cold<T, kAdjGlobal, false>(A, W, s0, s1, g, w, grad, lls, g_bar_acc);
         }

@@ -117,6 +117,12 @@ struct AdjointArgs {
     // and last clicks (adjoint_counts_kernel); null when not built.
     const uint4* tcnt;
     const int64_t* tcnt_off;
+    // Every session of each staged tile packed in click-mask order (the
+    // packing kernel's layout: uint16 [10][spad] window indices, uint16
+    // [spad] clicks at ptiles[t].blk_off), read for whole tiles; null when
+    // not built.
+    const TileDev* ptiles;
+    const unsigned char* pblk;
     double scale;            // gradient scale (the caller's grad_output)
     double* g_alpha;         // FP64 gradient accumulators
     double* g_beta;

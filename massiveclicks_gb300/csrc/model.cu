@@ -391,6 +391,11 @@ struct mc_model {
     int64_t adj_entries = 0;
     int64_t* d_adj_off = nullptr;
     uint4* d_adj_cnt = nullptr;
+    // Every session of each staged tile packed in click-mask order (the
+    // packing kernel's PBM layout, no session dropped), for the adjoint's
+    // whole tiles; built with the counts.
+    TileDev* d_adj_tiles = nullptr;
+    unsigned char* d_adj_blk = nullptr;
     int64_t adj_bytes = 0;
     // Launch shapes of the count kernels (entry kernel; dense PBM kernel).
     CountShape count_shape{8, 256, 8};
@@ -455,9 +460,11 @@ struct mc_model {
         tile_bytes = 0;
         tiles_ready = false;
         h_tile_begin.clear();
-        settle(d_adj_off, d_adj_cnt);
+        settle(d_adj_off, d_adj_cnt, d_adj_tiles, d_adj_blk);
         dfree(d_adj_off);
         dfree(d_adj_cnt);
+        dfree(d_adj_tiles);
+        dfree(d_adj_blk);
         bytes -= adj_bytes;
         adj_bytes = 0;
         h_adj_off.clear();
@@ -1856,6 +1863,8 @@ static AdjointArgs adjoint_args(mc_model* m, int64_t s_begin, int64_t s_count, c
     A.tcnt_off = nullptr;
     A.f_alpha = nullptr;
     A.f_beta = nullptr;
+    A.ptiles = nullptr;
+    A.pblk = nullptr;
     A.scale = scale;
     A.g_alpha = m->d_grad;
     A.g_beta = m->d_grad + m->qd_alloc();
@@ -1875,22 +1884,43 @@ static bool adjoint_tile_path(const mc_model* m) {
 // tile layout on the first call that takes the tile path.
 static int ensure_adjoint_counts(mc_model* m, cudaStream_t st) {
     if (!adjoint_tile_path(m) || m->adj_entries == 0 || m->d_adj_cnt) return MC_OK;
+    // The packed copy: the model's tile descriptors with every session of a
+    // staged tile kept (s_packed = s_count) and their own block offsets.
+    std::vector<TileDev> at((size_t)m->n_tiles);
+    CK(cudaMemcpy(at.data(), m->d_tiles, at.size() * sizeof(TileDev), cudaMemcpyDeviceToHost));
+    int64_t blk = 0;
+    int max_sessions = 1;
+    for (TileDev& t : at) {
+        t.blk_off = blk;
+        if (t.qd_count <= m->wqd) {
+            t.s_packed = t.s_count;
+            blk += 22 * (int64_t)((t.s_count + 7) & ~7);
+            max_sessions = std::max(max_sessions, t.s_count);
+        }
+    }
     const int64_t before = m->bytes;
     int rc = dalloc(&m->d_adj_off, m->h_adj_off.size(), &m->bytes);
     if (!rc) rc = dalloc(&m->d_adj_cnt, (size_t)m->adj_entries, &m->bytes);
+    if (!rc) rc = dalloc(&m->d_adj_tiles, at.size(), &m->bytes);
+    if (!rc) rc = dalloc(&m->d_adj_blk, (size_t)std::max<int64_t>(blk, 16), &m->bytes);
     if (rc) {
         dfree(m->d_adj_off);
         dfree(m->d_adj_cnt);
+        dfree(m->d_adj_tiles);
+        dfree(m->d_adj_blk);
         m->bytes = before;
         return rc;
     }
     m->adj_bytes = m->bytes - before;
     CK(cudaMemcpyAsync(m->d_adj_off, m->h_adj_off.data(), m->h_adj_off.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
                        st));
+    CK(cudaMemcpyAsync(m->d_adj_tiles, at.data(), at.size() * sizeof(TileDev), cudaMemcpyHostToDevice, st));
     CK(launch_adjoint_counts(m->d_tiles, m->n_tiles, m->wqd, m->d_pidx, m->d_click, m->stride, m->d_adj_off,
                              m->d_adj_cnt, m->n_sm, st));
-    CK(cudaStreamSynchronize(st));  // the host offsets stay alive meanwhile
-    return MC_OK;
+    CK(launch_pack_tiles(MC_PBM, m->d_adj_tiles, m->n_tiles, m->wqd, max_sessions, m->d_pidx, m->stride, m->d_click,
+                         m->d_adj_blk, m->d_status, m->n_sm, st));
+    CK(cudaStreamSynchronize(st));  // the host arrays stay alive meanwhile
+    return check_status(m, st);
 }
 
 // Gradient outputs.  The FP32 tile path writes the alpha and beta gradients
@@ -1929,6 +1959,8 @@ static cudaError_t run_adjoint(mc_model* m, const AdjointArgs& A0, bool grad, bo
         if (grad && !fp64 && m->d_adj_cnt) {
             A.tcnt = m->d_adj_cnt;
             A.tcnt_off = m->d_adj_off;
+            A.ptiles = m->d_adj_tiles;
+            A.pblk = m->d_adj_blk;
         }
         const auto& tb = m->h_tile_begin;
         // tiles [t0, t1) intersect [begin, begin + count): tile starts ascend
