@@ -1,6 +1,8 @@
-"""Device-block cache (csrc/host/devmem.cpp): a model created, fitted and
-destroyed again with the same sizes reuses the freed blocks and gets the same
-results; mc_empty_cache returns the blocks to the driver."""
+"""Device-block cache and page-locked host pool (csrc/host/devmem.cpp): a
+model created, fitted and destroyed again with the same sizes reuses the freed
+device blocks and the page-locked buffers its upload reads back into (segment
+ranges, has-a-click bits), both still holding the previous fit's data, and
+gets the same results; mc_empty_cache(-1) returns both to the driver."""
 import numpy as np
 import pytest
 
