@@ -683,22 +683,33 @@ int mc_model::build_tiles() {
     mch::parallel_for(n_chunks, [&](size_t c) {
         build_range(cut[c], cut[c + 1], chunk_tiles[c], chunk_splits[c], chunk_bins[c]);
     });
-    std::vector<TileDev> tiles;
-    std::vector<SplitDev> splits;
-    int64_t bin_off = 0;
+    // The chunks' tiles and splits in chunk order, each chunk copied into its
+    // place by the pool (one append after another took a third of the host
+    // tiling time).
+    std::vector<size_t> t_at(n_chunks + 1, 0), s_at(n_chunks + 1, 0);
+    std::vector<int64_t> b_at(n_chunks + 1, 0);
     for (size_t c = 0; c < n_chunks; c++) {
-        const int soff = (int)splits.size();
+        t_at[c + 1] = t_at[c] + chunk_tiles[c].size();
+        s_at[c + 1] = s_at[c] + chunk_splits[c].size();
+        b_at[c + 1] = b_at[c] + chunk_bins[c];
+    }
+    std::vector<TileDev> tiles(t_at[n_chunks]);
+    std::vector<SplitDev> splits(s_at[n_chunks]);
+    const int64_t bin_off = b_at[n_chunks];
+    mch::parallel_for(n_chunks, [&](size_t c) {
+        const int soff = (int)s_at[c];
+        TileDev* td = tiles.data() + t_at[c];
         for (TileDev t : chunk_tiles[c]) {
             if (t.split >= 0) t.split += soff;
-            tiles.push_back(t);
+            *td++ = t;
         }
+        SplitDev* sd = splits.data() + s_at[c];
         for (SplitDev sp : chunk_splits[c]) {
             sp.local += soff;
-            sp.bin_offset += bin_off;
-            splits.push_back(sp);
+            sp.bin_offset += b_at[c];
+            *sd++ = sp;
         }
-        bin_off += chunk_bins[c];
-    }
+    });
     // Packed session blocks of the staged (non-direct) tiles, 16-byte aligned.
     // Sized by the packed counts, which the packing kernel checks.
     int64_t blk = 0;
@@ -1873,8 +1884,6 @@ static AdjointArgs adjoint_args(mc_model* m, int64_t s_begin, int64_t s_count, c
     return A;
 }
 
-// Through the tiles when the sessions are grouped by query (tiles built),
-// else one thread per session with global atomics.
 // Sessions grouped by query with tiles built: the adjoint's tile path.
 static bool adjoint_tile_path(const mc_model* m) {
     return m->fused_ok && m->tiles_ready && !m->h_tile_begin.empty();
@@ -1953,6 +1962,8 @@ static cudaError_t adjoint_finish(mc_model* m, const AdjointArgs& A, float* d_al
     return e;
 }
 
+// Through the tiles when the sessions are grouped by query (tiles built),
+// else one thread per session with global atomics.
 static cudaError_t run_adjoint(mc_model* m, const AdjointArgs& A0, bool grad, bool fp64, cudaStream_t st) {
     AdjointArgs A = A0;
     if (adjoint_tile_path(m)) {
