@@ -64,6 +64,8 @@ def parse_args():
     ap.add_argument("--e2e-iters", type=int, default=50)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-models", action="store_true",
+                    help="skip timing the other three models on the same sessions")
     ap.add_argument("--no-train", action="store_true",
                     help="adjoint workload: skip EM's curve and Adam (EM and adjoint timing, gradient error only)")
     ap.add_argument("--no-autotune", action="store_true")
@@ -498,6 +500,30 @@ def run_ours(args, rank: int, world: int, local: int):
                "seconds_per_step_median": statistics.median(step_s), "steps": e2e_steps,
                "step": f"mc_model_create + mc_model_upload (pinned host sessions) + {args.e2e_iters} fused "
                        "iterations + mc_model_get_param of every array + destroy"}
+
+    # ---- the other models on the same sessions: fused EM, default tile shape,
+    # 200 iterations timed with CUDA events after 10 ---------------------------
+    if not args.no_models:
+        others = {}
+        for name in [k for k in ("pbm", "ubm", "ccm", "dbn") if k != args.model]:
+            om = api.ClickModel.create(MODELS[name], device=local)
+            om.upload(ds.train, n_qd, stream)
+            om.em(10, IMPL_FUSED, stream)
+            stream.synchronize()
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            om.em(200, IMPL_FUSED, stream)
+            ev1.record(stream)
+            ev1.synchronize()
+            ms = ev0.elapsed_time(ev1) / 200
+            survey_bytes = 42 * n_train + (80 if name == "dbn" else 40) * n_qd
+            path, _ = om.fused_path()
+            others[name] = {"ms_per_iteration": ms, "session_iterations_per_s": world * n_train / (ms / 1e3),
+                            "roofline_frac_survey_bytes": survey_bytes / (ms / 1e3) / 1e9 / hbm,
+                            "path": path}
+            om.destroy_parameters()
+        out["other_models"] = others
 
     cpu = None
     if rank == 0 and not args.no_cpu:
