@@ -12,7 +12,9 @@
 // (reverse mode) to the adjoints of a, s and g; the messages are recomputed
 // by every call instead of being stored.  Sessions grouped by query go
 // through the model's tiles, with the gradient summed per tile in shared
-// memory; other session orders through FP64 global atomics per session.
+// memory (FP32: fixed-point bins, constant terms counted, whole tiles read a
+// packed copy of their sessions in click-mask order); other session orders
+// through FP64 global atomics per session.
 #include <cstdint>
 #include <map>
 #include <mutex>
