@@ -186,6 +186,35 @@ def test_fp32_counted_terms_whole_and_cut_tiles():
         np.testing.assert_allclose(got, b64, rtol=1e-4, atol=1e-5)
 
 
+def test_fp32_small_windows_of_split_queries():
+    """Queries with thousands of sessions over a few dozen documents are split
+    over several tiles whose windows (at most 30 pairs) take the small-window
+    layout (per-(warp, lane % 4) copies of the bins), read from the packed
+    copy for whole tiles and with count atomics for a tile a range cuts.  The
+    FP32 gradient matches FP64 at the FP32 bar in both."""
+    cfg = api.synth_config(1, n_sessions=100_000, n_queries=20, pool=30, seed=91)
+    q, d, m = api.synth_sessions(cfg)
+    ds = api.Dataset.from_sessions(q, d, m, 0.2)
+    cm = api.DBNModel()
+    cm.upload(ds.train, ds.n_qd)
+    assert cm.fused_path()[0] == "tiles"
+    rng = np.random.default_rng(12)
+    al = rng.normal(-1.0, 1.0, ds.n_qd).astype(np.float32)
+    be = rng.normal(-1.0, 1.0, ds.n_qd).astype(np.float32)
+    ga = np.array([1.5], np.float32)
+    n = cm.n_train
+    a64, b64, g64 = _grads_range(cm, al, be, ga, 0, n, fp64=True)
+    a32, b32, g32 = _grads_range(cm, al, be, ga, 0, n)
+    cut = n // 3 + 101
+    a1, b1, _ = _grads_range(cm, al, be, ga, 0, cut)
+    a2, b2, _ = _grads_range(cm, al, be, ga, cut, n - cut)
+    for got in (a32, a1 + a2):
+        np.testing.assert_allclose(got, a64, rtol=1e-4, atol=1e-5)
+    for got in (b32, b1 + b2):
+        np.testing.assert_allclose(got, b64, rtol=1e-4, atol=1e-5)
+    assert g32 == pytest.approx(g64, rel=1e-4)
+
+
 def test_ranges_add_up():
     case, cm, al, be, ga = _setup(seed=5)
     dev = torch.device("cuda", 0)
