@@ -465,16 +465,26 @@ def run_ours(args, rank: int, world: int, local: int):
         import ctypes as C
 
         def e2e_step():
+            """One end-to-end step; returns its phase times (host clock, each
+            phase synchronised on the stream)."""
+            t = [time.perf_counter()]
             m2 = C.c_void_p()
             api.check(lib.mc_model_create(MODELS[args.model], 0, local, C.byref(m2)))
             api.check(lib.mc_model_upload(m2, n_train, C.c_void_p(pq.data_ptr()), C.c_void_p(pp.data_ptr()),
                                           C.c_void_p(pm.data_ptr()), n_qd, C.c_void_p(stream.cuda_stream)))
             api.check(lib.mc_model_configure(m2, spt, wqd, block))
+            stream.synchronize()
+            t.append(time.perf_counter())
             api.check(lib.mc_model_em(m2, args.e2e_iters, IMPL_FUSED, C.c_void_p(stream.cuda_stream)))
+            stream.synchronize()
+            t.append(time.perf_counter())
             for i, (name, _) in enumerate(sizes):
                 api.check(lib.mc_model_get_param(m2, i, C.c_void_p(host_out[name].data_ptr()),
                                                  C.c_void_p(stream.cuda_stream)))
             lib.mc_model_destroy(m2)
+            t.append(time.perf_counter())
+            return {"create_upload_ms": 1e3 * (t[1] - t[0]), "iterations_ms": 1e3 * (t[2] - t[1]),
+                    "download_destroy_ms": 1e3 * (t[3] - t[2])}
 
         e2e_step()  # warm-up (the first upload of a process also allocates the library's caches)
         torch.cuda.synchronize()
@@ -485,19 +495,22 @@ def run_ours(args, rank: int, world: int, local: int):
         import gc
         gc.collect()
         gc.disable()
-        e2e_steps = 10
-        step_s = []
+        e2e_steps = 20
+        step_s, phases = [], []
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
             t1 = time.perf_counter()
-            e2e_step()
+            phases.append(e2e_step())
             step_s.append(time.perf_counter() - t1)
         torch.cuda.synchronize()
         e2e_s = dist.max((time.perf_counter() - t0) / e2e_steps)
         gc.enable()
+        slowest = max(range(e2e_steps), key=lambda i: step_s[i])
         e2e = {"value": world * n_train * args.e2e_iters / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_s,
                "seconds_per_step_median": statistics.median(step_s), "steps": e2e_steps,
+               "phases_median_ms": {k: round(statistics.median(p[k] for p in phases), 3) for k in phases[0]},
+               "slowest_step_phases_ms": {k: round(v, 3) for k, v in phases[slowest].items()},
                "step": f"mc_model_create + mc_model_upload (pinned host sessions) + {args.e2e_iters} fused "
                        "iterations + mc_model_get_param of every array + destroy"}
 
