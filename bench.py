@@ -511,6 +511,7 @@ def run_ours(args, rank: int, world: int, local: int):
                "seconds_per_step_median": statistics.median(step_s), "steps": e2e_steps,
                "phases_median_ms": {k: round(statistics.median(p[k] for p in phases), 3) for k in phases[0]},
                "slowest_step_phases_ms": {k: round(v, 3) for k, v in phases[slowest].items()},
+               "slowest_step_index": slowest,
                "step": f"mc_model_create + mc_model_upload (pinned host sessions) + {args.e2e_iters} fused "
                        "iterations + mc_model_get_param of every array + destroy"}
 
